@@ -1,0 +1,248 @@
+/*
+ * ncgb300.h -- C ABI of the GB300 (sm_103a) device path for ncarray arrays.
+ *
+ * Every entry point takes plain pointers, sizes and an explicit CUDA stream
+ * (a cudaStream_t passed as void*; NULL = legacy default stream). No call
+ * synchronises the device or throws: each returns an nca_status and, on
+ * failure, nca_last_error() returns a message for the calling thread.
+ *
+ * The entry points replace the device seam of ncarray v0.7.8:
+ *   - ncarray::GPUEngine static functions   src/lib/ncarray/engines/gpuengine.hh:64-638
+ *   - device::RuntimeCompiler (NVRTC JIT)   src/lib/ncarray/jit/device/rtcompiler.hh:94-161
+ *   - ncarray::Stencil<NDIM>                src/lib/ncarray/expression/stencil.hh:58-255
+ *   - device scatter_add (histogram seed)   src/lib/ncarray/device/kernels.cuh:660-680
+ * Each declaration below names the reference function it stands in for.
+ */
+#ifndef NCGB300_H
+#define NCGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NCA_MAX_NDIM 10   /* NCARRAY_MAX_NDIM, src/lib/ncarray/custom_types.hh:65-67 */
+#define NCA_MAX_OPERANDS 24
+#define NCA_MAX_SCALARS 32
+#define NCA_MAX_INSTRS 128
+#define NCA_MAX_REDUCTIONS 4
+
+/* ---- status codes -------------------------------------------------------- */
+typedef enum nca_status {
+  NCA_OK = 0,
+  NCA_ERR_INVALID = 1,      /* null pointer, bad descriptor, bad tape            */
+  NCA_ERR_DTYPE = 2,        /* dtype not supported by this operation             */
+  NCA_ERR_SHAPE = 3,        /* shapes do not broadcast / reduce as requested     */
+  NCA_ERR_COMPILE = 4,      /* NVRTC failed; nca_last_error() holds the log head */
+  NCA_ERR_CUDA = 5,         /* a CUDA runtime/driver call failed                 */
+  NCA_ERR_OOM = 6,          /* device scratch allocation failed                  */
+  NCA_ERR_TIMEOUT = 7,      /* a bounded device wait gave up (status word set)   */
+  NCA_ERR_UNSUPPORTED = 8,  /* valid request this build does not implement       */
+  NCA_ERR_LIMIT = 9         /* a size limit of this ABI was exceeded             */
+} nca_status;
+
+/* ---- dtypes: numbering of ncarray::DType (src/lib/ncarray/dtype.hh:56-80),
+ *      plus two 16-bit float storage types the reference does not have. ---- */
+typedef enum nca_dtype {
+  NCA_BOOL = 0, NCA_CHAR = 1, NCA_UINT8 = 2, NCA_UINT16 = 3, NCA_UINT32 = 4,
+  NCA_UINT64 = 5, NCA_INT8 = 6, NCA_INT16 = 7, NCA_INT32 = 8, NCA_INT64 = 9,
+  NCA_FLOAT32 = 10, NCA_FLOAT64 = 11,
+  /* 12..21: float128, complex and vector dtypes -- not on the device path */
+  NCA_BFLOAT16 = 22, NCA_FLOAT16 = 23
+} nca_dtype;
+
+/* ---- opcodes: numbering of ncarray::OpCode (src/lib/ncarray/op_code.hh:47-84),
+ *      with ABS and SQRT appended after RSHFT. Instructions are packed as in
+ *      pack_instruction (op_code.hh:164-168): (op << 24) | (operand index). -- */
+typedef enum nca_opcode {
+  NCA_OP_NOOP = 0, NCA_OP_IDX = 1, NCA_OP_LOAD_NCARR = 2, NCA_OP_LOAD_SOARR = 3,
+  NCA_OP_LOAD_CONST = 4, NCA_OP_NEG = 5, NCA_OP_INC = 6, NCA_OP_DEC = 7,
+  NCA_OP_SZOF = 8, NCA_OP_ADDR = 9, NCA_OP_INDR = 10, NCA_OP_CAST = 11,
+  NCA_OP_LNOT = 12, NCA_OP_BNOT = 13, NCA_OP_ADD = 14, NCA_OP_SUB = 15,
+  NCA_OP_MUL = 16, NCA_OP_DIV = 17, NCA_OP_MOD = 18, NCA_OP_FDIV = 19,
+  NCA_OP_EQ = 20, NCA_OP_NE = 21, NCA_OP_LT = 22, NCA_OP_LE = 23, NCA_OP_GT = 24,
+  NCA_OP_GE = 25, NCA_OP_LAND = 26, NCA_OP_LOR = 27, NCA_OP_BAND = 28,
+  NCA_OP_BOR = 29, NCA_OP_XOR = 30, NCA_OP_LSHFT = 31, NCA_OP_RSHFT = 32,
+  NCA_OP_ABS = 34, NCA_OP_SQRT = 35
+} nca_opcode;
+
+/* ---- reductions: SumTraits..MeanTraits (src/lib/ncarray/reductions.hh:109-381) */
+typedef enum nca_reduce_op {
+  NCA_RED_SUM = 0,     /* out dtype = op_traits<T>::sum_type (bf16/fp16 -> f32)  */
+  NCA_RED_MEAN = 1,    /* out dtype = float64 (sum / count)                      */
+  NCA_RED_MAX = 2,     /* out dtype = T                                          */
+  NCA_RED_MIN = 3,     /* out dtype = T                                          */
+  NCA_RED_ARGMAX = 4,  /* out dtype = int64, index along the reduced axes        */
+  NCA_RED_ARGMIN = 5   /* out dtype = int64                                      */
+} nca_reduce_op;
+
+/*
+ * An N-d view: NCOffsetsPolicy semantics (src/lib/ncarray/layout.hh:451-535).
+ * Element address = data + sum_k (idx_k * strides[k] + offsets[k]) for every
+ * axis k, except that on `pointer_axis` (if >= 0) the running pointer is read
+ * as a void* table: p = ((void**)p)[idx + offsets[axis] / sizeof(void*)]...
+ * (pointer axes are rejected with NCA_ERR_UNSUPPORTED by this build).
+ * Strides and offsets are in BYTES; stride 0 broadcasts an axis.
+ */
+typedef struct nca_view {
+  void* data;
+  int32_t dtype;
+  int32_t ndim;
+  int64_t shape[NCA_MAX_NDIM];
+  int64_t strides[NCA_MAX_NDIM];
+  int64_t offsets[NCA_MAX_NDIM];
+  int32_t pointer_axis;
+  int32_t flags;            /* reserved, must be 0 */
+} nca_view;
+
+/*
+ * An expression tape: the RPN program of ncarray::ExprMVNode
+ * (src/lib/ncarray/expression/mvnode.hh:82-459). LOAD_NCARR/LOAD_SOARR index
+ * the operand views, LOAD_CONST the scalars. Every value of the tape is
+ * evaluated in `compute_dtype` (the reference's WorkT: the result dtype, or
+ * the promoted work dtype when the result is bool -- dynamicmvnode.hh:146-251)
+ * and the result is cast to the output view's dtype.
+ * Scalars are passed as 8-byte slots: scalar i has dtype scalar_dtypes[i] and
+ * its value in the first itemsize bytes of scalar_slots[i].
+ */
+typedef struct nca_tape {
+  const uint32_t* instrs;
+  int32_t n_instrs;
+  int32_t n_scalars;
+  const int32_t* scalar_dtypes;
+  const uint64_t* scalar_slots;
+  int32_t compute_dtype;
+  int32_t result_dtype;     /* dtype of the expression value fed to reductions */
+} nca_tape;
+
+/* One reduction of an expression (or of a single view). */
+typedef struct nca_reduction {
+  int32_t op;               /* nca_reduce_op                                    */
+  uint32_t axes_mask;       /* bit k = reduce logical axis k; all bits = full   */
+  nca_view out;             /* result: shape = kept axes in order (0-d if full) */
+} nca_reduction;
+
+/* ---- library ------------------------------------------------------------- */
+const char* nca_last_error(void);
+int32_t nca_version(void);
+/* Number of kernels launched by this library in this process (all entry points). */
+int64_t nca_launch_count(void);
+/* Number of JIT kernels compiled / loaded from the disk cache / found in memory. */
+int32_t nca_jit_stats(int64_t* compiled, int64_t* disk_hits, int64_t* mem_hits);
+/* Directory of the on-disk cubin cache (NULL resets to the default). Replaces
+ * the ~/.cache/ncarray lookup of src/lib/ncarray/jit/path_utils.cc:31-50. */
+int32_t nca_jit_set_cache_dir(const char* dir);
+/* Diagnostic: generates one kernel of every JIT class and compiles it with
+ * NVRTC for `arch` (e.g. "sm_103a") without touching a device. No reference
+ * counterpart (the reference only compiles on first use, rtcompiler.cc:445-510). */
+int32_t nca_jit_selftest(const char* arch, int32_t* n_compiled);
+
+/* ---- elementwise --------------------------------------------------------- */
+/* out[...] = tape(operands...) over the broadcast of the operands to out's shape.
+ * Replaces GPUEngine::execute_binary_expression (gpuengine.hh:90-195) with
+ * device::RuntimeCompiler::get_expr_kernel / get_dynamic_vm_kernel
+ * (rtcompiler.cc:49-89, :341-366). */
+int32_t nca_expr_eval(const nca_tape* tape, const nca_view* operands, int32_t n_operands,
+                      const nca_view* out, void* stream);
+
+/* One pass that evaluates the tape and (optionally) stores it to `expr_out`
+ * while computing up to NCA_MAX_REDUCTIONS reductions of its value over the
+ * same axes. The reference materialises the expression and then runs
+ * GPUEngine::execute_reduce_axes / execute_full_reduce on it
+ * (array_operations.hh:42-63,512-551,904-921); this fuses both. expr_out may
+ * be NULL. All reductions must share one axes_mask. The logical shape is the
+ * broadcast shape of the operands (or expr_out's shape when given). */
+int32_t nca_expr_reduce(const nca_tape* tape, const nca_view* operands, int32_t n_operands,
+                        const nca_view* expr_out, const nca_reduction* reds,
+                        int32_t n_reds, void* stream);
+
+/* Reduction of one view: GPUEngine::execute_reduce_axes (gpuengine.hh:222-288)
+ * when axes_mask is partial, GPUEngine::execute_full_reduce (:301-333) when it
+ * covers every axis. */
+int32_t nca_reduce(const nca_view* src, int32_t op, uint32_t axes_mask,
+                   const nca_view* out, void* stream);
+
+/* dst = cast(src) view to view: GPUEngine::execute_assign / execute_copy_into
+ * (gpuengine.hh:377-637; kernels.cuh:613-644). */
+int32_t nca_copy(const nca_view* src, const nca_view* dst, void* stream);
+
+/* dst[...] = cast(scalar): GPUEngine::execute_fill (gpuengine.hh:338-376). */
+int32_t nca_fill(const nca_view* dst, int32_t scalar_dtype, const void* scalar, void* stream);
+
+/* ---- 3-D stencils ---------------------------------------------------------- */
+/* dst[c] = src[c] + dt * sum_{o in 3x3x3} w[o] * src[c + o] with zero halo
+ * (out-of-grid neighbours read 0). weights[27] is indexed (dz+1)*9+(dy+1)*3+(dx+1);
+ * a 7-point stencil sets the 20 edge/corner weights to 0. src and dst are
+ * C-contiguous (nz, ny, nx) float32 or float64 grids, distinct buffers.
+ * Replaces the device-only Stencil<3>::create/apply of a sum of shifted views
+ * (stencil.hh:76-243; rtcompiler.hh:187-385). */
+int32_t nca_stencil3d(const nca_view* src, const nca_view* dst, const double* weights27,
+                      double dt, void* stream);
+/* `iters` Jacobi steps ping-ponging between a and b; the result ends in a if
+ * iters is even, else in b. */
+int32_t nca_stencil3d_iterate(const nca_view* a, const nca_view* b, const double* weights27,
+                              double dt, int32_t iters, void* stream);
+
+/* ---- 2-D histogram ---------------------------------------------------------- */
+/* For each point i with x_i, y_i finite: ix = floor((x_i - x_lo) * sx),
+ * iy = floor((y_i - y_lo) * sy) evaluated in float32 with sx = (float)(nbx/(x_hi-x_lo)),
+ * sy likewise; points with ix or iy outside [0, nb) are dropped.
+ * counts[iy*nbx + ix] += 1 (uint64, exact) and, when w != NULL,
+ * wsum[iy*nbx + ix] += w_i (float32 output, accumulated in float64).
+ * counts/wsum are ACCUMULATED into (zero them first for a fresh histogram).
+ * Stands in for the scatter_add primitive (kernels.cuh:660-680;
+ * host/elementwise.hh:482-505), which has no public API in the reference. */
+int32_t nca_hist2d(const float* x, const float* y, const float* w, int64_t n,
+                   int32_t nbx, int32_t nby, double x_lo, double x_hi, double y_lo,
+                   double y_hi, uint64_t* counts, float* wsum, void* stream);
+
+/* ---- batched uneven reductions -------------------------------------------- */
+/* One array of a batch: data pointer, length, dtype (float32/bfloat16/float16). */
+typedef struct nca_batch_item {
+  const void* data;
+  int64_t length;
+  int32_t dtype;
+  int32_t reserved;
+} nca_batch_item;
+
+/* Per-array results of nca_batch_reduce (float64, one row per array). */
+typedef struct nca_batch_result {
+  double sum;        /* sum(x)          */
+  double mean;       /* sum(x) / length */
+  double max;        /* max(x)          */
+  double sum_sq_m;   /* sum(x*x - x)    */
+} nca_batch_result;
+
+/* A prepared batch: device-side work-descriptor table, schedule and (after the
+ * first launch) an instantiated CUDA graph for the persistent kernel. */
+typedef struct nca_batch nca_batch;
+
+/* Builds the descriptor table for `items` (copied to the device on `stream`).
+ * The schedule (chunk size, block size, items per thread) comes from the
+ * autotuner cache when present, else from defaults. There is no reference
+ * counterpart: ncarray has no batched API (pyncarray/utilities.hh:271-314). */
+int32_t nca_batch_create(const nca_batch_item* items, int32_t n_items, nca_batch** out,
+                         void* stream);
+/* Runs the persistent batched kernel: results[i] for items[i] (device memory). */
+int32_t nca_batch_reduce(nca_batch* batch, nca_batch_result* results, void* stream);
+/* Same as nca_batch_reduce, replayed through a CUDA graph captured on first use. */
+int32_t nca_batch_reduce_graph(nca_batch* batch, nca_batch_result* results, void* stream);
+/* The plain form: per array, one launch per op with float64 accumulation. */
+int32_t nca_batch_reduce_plain(nca_batch* batch, nca_batch_result* results, void* stream);
+/* Times candidate schedules on `stream` and stores the best for this batch's
+ * shape class in the autotuner cache (file under the JIT cache directory). */
+int32_t nca_batch_autotune(nca_batch* batch, nca_batch_result* results, void* stream);
+/* Reports the schedule in use: chunk elements, threads per block, items per thread, CTAs. */
+int32_t nca_batch_schedule(const nca_batch* batch, int64_t* chunk, int32_t* threads,
+                           int32_t* items_per_thread, int32_t* ctas);
+/* Status word of the last launch (0 = ok, nonzero = a bounded wait gave up). */
+int32_t nca_batch_status(nca_batch* batch, int32_t* status, void* stream);
+void nca_batch_destroy(nca_batch* batch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NCGB300_H */

@@ -1,0 +1,590 @@
+"""Device arrays and lazy expressions with ncarray's Python surface.
+
+Mirrors the classes of ncarray's ``_pyncdevarray`` module
+(src/lib/pyncarray/ncdevarray.cu:47-58, binding_builder.hh:163-815):
+``NCDevArray`` (owner or view over device memory), ``DevExpr`` (the lazy tape
+of ExprMVNode, expression/mvnode.hh:82-459), the operator set, reductions
+``sum/mean/max/min/argmax/argmin`` with and without axes, ``fill``,
+``to_host``/``to_device`` and ``__array__``. Every device operation goes
+through the C ABI of libncgb300; device memory is a torch byte buffer.
+"""
+from __future__ import annotations
+
+import contextlib
+import ctypes
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from .dtype import (DType, FLOATS, ITEMSIZE, OpCode, RedOp, arith, compute_dtype, promote,
+                    result_dtype, scalar_dtype, scalar_slot, sum_type, to_numpy)
+
+_EAGER = [True]
+
+
+def set_eager(flag: bool) -> None:
+    """Eager mode materialises every operator result (ncarray's default)."""
+    _EAGER[0] = bool(flag)
+
+
+@contextlib.contextmanager
+def lazy_mode():
+    """Operators return DevExpr tapes that fuse into one kernel on use."""
+    old = _EAGER[0]
+    _EAGER[0] = False
+    try:
+        yield
+    finally:
+        _EAGER[0] = old
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def current_stream() -> int:
+    torch = _torch()
+    return int(torch.cuda.current_stream().cuda_stream)
+
+
+def _device():
+    torch = _torch()
+    if not torch.cuda.is_available():
+        raise RuntimeError("ncarray_gb300 device arrays need a CUDA device")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _c_strides(shape: Sequence[int], itemsize: int) -> list[int]:
+    st, acc = [], itemsize
+    for n in reversed(shape):
+        st.append(acc)
+        acc *= max(int(n), 1)
+    return list(reversed(st))
+
+
+class NCDevArray:
+    """An N-d device array (owner, or a strided view sharing an owner's buffer)."""
+
+    def __init__(self, shape: Sequence[int] = (), dtype: DType = DType.float64, *, _buf=None,
+                 _offset: int = 0, _strides: Optional[Sequence[int]] = None):
+        self.dtype = DType(dtype)
+        self.shape = tuple(int(n) for n in shape)
+        isz = ITEMSIZE[self.dtype]
+        if _buf is None:
+            nbytes = max(self.size * isz, 1)
+            _buf = _torch().empty(nbytes, dtype=_torch().uint8, device=_device())
+        self._buf = _buf
+        self._offset = int(_offset)
+        self.strides = tuple(int(s) for s in (_strides if _strides is not None else _c_strides(self.shape, isz)))
+
+    # ---- metadata ----
+    @property
+    def ndim(self) -> int:
+        return len(self.shape)
+
+    @property
+    def size(self) -> int:
+        n = 1
+        for e in self.shape:
+            n *= e
+        return n
+
+    @property
+    def itemsize(self) -> int:
+        return ITEMSIZE[self.dtype]
+
+    @property
+    def nbytes(self) -> int:
+        return self.size * self.itemsize
+
+    @property
+    def ptr(self) -> int:
+        return int(self._buf.data_ptr()) + self._offset
+
+    def is_contiguous(self) -> bool:
+        return list(self.strides) == _c_strides(self.shape, self.itemsize)
+
+    def view_struct(self) -> _lib.View:
+        return _lib.make_view(self.ptr, self.dtype, self.shape, self.strides)
+
+    def __len__(self) -> int:
+        return self.shape[0]
+
+    def __repr__(self) -> str:
+        return f"NCDevArray(shape={self.shape}, dtype={self.dtype.name})"
+
+    # ---- construction ----
+    @classmethod
+    def empty(cls, shape: Sequence[int], dtype: DType) -> "NCDevArray":
+        return cls(shape, dtype)
+
+    @classmethod
+    def from_host(cls, arr: np.ndarray, dtype: Optional[DType] = None) -> "NCDevArray":
+        """Copies a numpy array to a new C-contiguous device owner.
+        bfloat16 data is passed as uint16 bit patterns with dtype=DType.bfloat16."""
+        from .dtype import from_numpy
+        a = np.ascontiguousarray(arr)
+        dt = DType(dtype) if dtype is not None else from_numpy(a.dtype)
+        if ITEMSIZE[dt] != a.itemsize:
+            raise TypeError(f"{a.dtype} cannot hold {dt.name}")
+        out = cls(a.shape, dt)
+        if a.size:
+            torch = _torch()
+            src = torch.from_numpy(a.reshape(-1).view(np.uint8))
+            out._buf[: a.nbytes].copy_(src, non_blocking=False)
+        return out
+
+    def to_host(self) -> np.ndarray:
+        """Copies to a new C-contiguous numpy array (synchronises)."""
+        src = self if self.is_contiguous() else self.copy()
+        npdt = to_numpy(self.dtype)
+        if src.size == 0:
+            return np.zeros(self.shape, dtype=npdt)
+        raw = src._buf[src._offset: src._offset + src.nbytes].cpu().numpy()
+        return raw.view(npdt).reshape(self.shape)
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.to_host()
+        return a.astype(dtype) if dtype is not None else a
+
+    # ---- views ----
+    def transpose(self, *axes) -> "NCDevArray":
+        if len(axes) == 1 and isinstance(axes[0], (tuple, list)):
+            axes = tuple(axes[0])
+        if not axes:
+            axes = tuple(reversed(range(self.ndim)))
+        if sorted(axes) != list(range(self.ndim)):
+            raise ValueError("axes must be a permutation")
+        return NCDevArray([self.shape[a] for a in axes], self.dtype, _buf=self._buf,
+                          _offset=self._offset, _strides=[self.strides[a] for a in axes])
+
+    permute = transpose
+
+    def reshape(self, *shape) -> "NCDevArray":
+        if len(shape) == 1 and isinstance(shape[0], (tuple, list)):
+            shape = tuple(shape[0])
+        shape = list(shape)
+        if -1 in shape:
+            known = 1
+            for s in shape:
+                if s != -1:
+                    known *= s
+            shape[shape.index(-1)] = self.size // known
+        n = 1
+        for s in shape:
+            n *= s
+        if n != self.size:
+            raise ValueError("reshape changes the size")
+        src = self if self.is_contiguous() else self.copy()
+        return NCDevArray(shape, self.dtype, _buf=src._buf, _offset=src._offset)
+
+    def broadcast_to(self, shape: Sequence[int]) -> "NCDevArray":
+        shape = tuple(shape)
+        pad = len(shape) - self.ndim
+        st = [0] * pad + list(self.strides)
+        sh = [1] * pad + list(self.shape)
+        for d in range(len(shape)):
+            if sh[d] == 1 and shape[d] != 1:
+                st[d] = 0
+            elif sh[d] != shape[d]:
+                raise ValueError("cannot broadcast")
+        return NCDevArray(shape, self.dtype, _buf=self._buf, _offset=self._offset, _strides=st)
+
+    def __getitem__(self, key) -> "NCDevArray":
+        if not isinstance(key, tuple):
+            key = (key,)
+        if Ellipsis in key:
+            i = key.index(Ellipsis)
+            key = key[:i] + (slice(None),) * (self.ndim - len(key) + 1) + key[i + 1:]
+        shape, strides, off = [], [], self._offset
+        d = 0
+        for k in key:
+            if k is None:
+                shape.append(1)
+                strides.append(0)
+                continue
+            n, s = self.shape[d], self.strides[d]
+            if isinstance(k, slice):
+                start, stop, step = k.indices(n)
+                cnt = max(0, (stop - start + (step - (1 if step > 0 else -1))) // step)
+                off += start * s
+                shape.append(cnt)
+                strides.append(s * step)
+            else:
+                i = int(k)
+                if i < 0:
+                    i += n
+                if not 0 <= i < n:
+                    raise IndexError("index out of range")
+                off += i * s
+            d += 1
+        shape += list(self.shape[d:])
+        strides += list(self.strides[d:])
+        return NCDevArray(shape, self.dtype, _buf=self._buf, _offset=off, _strides=strides)
+
+    def __setitem__(self, key, value) -> None:
+        self[key].assign(value)
+
+    # ---- copies ----
+    def copy(self) -> "NCDevArray":
+        out = NCDevArray(self.shape, self.dtype)
+        out.assign(self)
+        return out
+
+    def astype(self, dtype: DType) -> "NCDevArray":
+        out = NCDevArray(self.shape, dtype)
+        out.assign(self)
+        return out
+
+    def assign(self, other) -> "NCDevArray":
+        """Casting copy into this view (broadcasting `other`)."""
+        if isinstance(other, DevExpr):
+            other.evaluate(out=self)
+            return self
+        if isinstance(other, np.ndarray):
+            other = NCDevArray.from_host(other)
+        if isinstance(other, NCDevArray):
+            if self.size:
+                _lib.call("nca_copy", ctypes.byref(other.view_struct()), ctypes.byref(self.view_struct()),
+                          current_stream())
+            return self
+        return self.fill(other)
+
+    def fill(self, value) -> "NCDevArray":
+        dt = scalar_dtype(value)
+        slot = ctypes.c_uint64(scalar_slot(value, dt))
+        if self.size:
+            _lib.call("nca_fill", ctypes.byref(self.view_struct()), int(dt), ctypes.byref(slot), current_stream())
+        return self
+
+    # ---- expressions ----
+    def _expr(self) -> "DevExpr":
+        return DevExpr.leaf(self)
+
+    # ---- reductions ----
+    def sum(self, axes=None):
+        return self._expr().sum(axes)
+
+    def mean(self, axes=None):
+        return self._expr().mean(axes)
+
+    def max(self, axes=None):
+        return self._expr().max(axes)
+
+    def min(self, axes=None):
+        return self._expr().min(axes)
+
+    def argmax(self, axes=None):
+        return self._expr().argmax(axes)
+
+    def argmin(self, axes=None):
+        return self._expr().argmin(axes)
+
+
+def _as_node(x):
+    if isinstance(x, DevExpr):
+        return x
+    if isinstance(x, NCDevArray):
+        return DevExpr.leaf(x)
+    if isinstance(x, np.ndarray):
+        return DevExpr.leaf(NCDevArray.from_host(x))
+    return DevExpr.const(x)
+
+
+class DevExpr:
+    """A lazy tape (RPN instructions over array operands and scalars)."""
+
+    def __init__(self):
+        self.arrays: list[NCDevArray] = []
+        self.scalars: list[tuple[DType, int]] = []
+        self.instrs: list[int] = []
+        self.work: Optional[DType] = None
+        self.expr_dtype: Optional[DType] = None
+
+    # ---- building (ExprMVNode::build_node) ----
+    @classmethod
+    def leaf(cls, a: NCDevArray) -> "DevExpr":
+        e = cls()
+        e.arrays.append(a)
+        e.instrs.append((OpCode.LOAD_NCARR << 24) | 0)
+        e.work = e.expr_dtype = a.dtype
+        return e
+
+    @classmethod
+    def const(cls, v) -> "DevExpr":
+        e = cls()
+        dt = scalar_dtype(v)
+        e.scalars.append((dt, scalar_slot(v, dt)))
+        e.instrs.append((OpCode.LOAD_CONST << 24) | 0)
+        e.work = e.expr_dtype = dt
+        return e
+
+    @classmethod
+    def iota(cls, like: "NCDevArray | Sequence[int]", dtype: DType = DType.int64) -> "DevExpr":
+        """The IDX generator: the C-order linear index of each element."""
+        shape = like.shape if isinstance(like, NCDevArray) else tuple(like)
+        e = cls()
+        e.instrs.append(OpCode.IDX << 24)
+        e.work = e.expr_dtype = DType(dtype)
+        e._iota_shape = tuple(shape)
+        return e
+
+    def _append(self, other: "DevExpr") -> None:
+        na, ns = len(self.arrays), len(self.scalars)
+        self.arrays += other.arrays
+        self.scalars += other.scalars
+        for ins in other.instrs:
+            op, idx = ins >> 24, ins & 0xFFFFFF
+            if op in (OpCode.LOAD_NCARR, OpCode.LOAD_SOARR):
+                ins = (op << 24) | (idx + na)
+            elif op == OpCode.LOAD_CONST:
+                ins = (op << 24) | (idx + ns)
+            self.instrs.append(ins)
+        if getattr(other, "_iota_shape", None) is not None and getattr(self, "_iota_shape", None) is None:
+            self._iota_shape = other._iota_shape
+
+    def _clone(self) -> "DevExpr":
+        e = DevExpr()
+        e.arrays = list(self.arrays)
+        e.scalars = list(self.scalars)
+        e.instrs = list(self.instrs)
+        e.work, e.expr_dtype = self.work, self.expr_dtype
+        if getattr(self, "_iota_shape", None) is not None:
+            e._iota_shape = self._iota_shape
+        return e
+
+    def _binary(self, op: OpCode, other, reverse: bool = False):
+        a, b = (self, _as_node(other)) if not reverse else (_as_node(other), self)
+        e = a._clone()
+        e._append(b)
+        e.work = promote(a.work, b.work)
+        e.expr_dtype = result_dtype(op, e.work)
+        e.instrs.append(op << 24)
+        return e._finish()
+
+    def _unary(self, op: OpCode):
+        e = self._clone()
+        e.expr_dtype = result_dtype(op, e.work)
+        e.instrs.append(op << 24)
+        return e._finish()
+
+    def _finish(self):
+        return self.materialize() if _EAGER[0] else self
+
+    # ---- evaluation ----
+    @property
+    def dtype(self) -> DType:
+        return self.expr_dtype
+
+    @property
+    def shape(self) -> tuple:
+        shapes = [a.shape for a in self.arrays]
+        if getattr(self, "_iota_shape", None) is not None:
+            shapes.append(self._iota_shape)
+        n = max((len(s) for s in shapes), default=0)
+        out = [1] * n
+        for s in shapes:
+            for d, e in enumerate(s):
+                ld = d + n - len(s)
+                if e != 1:
+                    if out[ld] not in (1, e):
+                        raise ValueError("operands do not broadcast")
+                    out[ld] = e
+        return tuple(out)
+
+    def _tape(self):
+        ins = (ctypes.c_uint32 * max(len(self.instrs), 1))(*self.instrs)
+        sd = (ctypes.c_int32 * max(len(self.scalars), 1))(*[int(d) for d, _ in self.scalars])
+        ss = (ctypes.c_uint64 * max(len(self.scalars), 1))(*[s for _, s in self.scalars])
+        t = _lib.Tape()
+        t.instrs = ctypes.cast(ins, ctypes.POINTER(ctypes.c_uint32))
+        t.n_instrs = len(self.instrs)
+        t.n_scalars = len(self.scalars)
+        t.scalar_dtypes = ctypes.cast(sd, ctypes.POINTER(ctypes.c_int32))
+        t.scalar_slots = ctypes.cast(ss, ctypes.POINTER(ctypes.c_uint64))
+        t.compute_dtype = int(compute_dtype(self.expr_dtype, self.work))
+        t.result_dtype = int(self.expr_dtype)
+        return t, (ins, sd, ss)
+
+    def _operands(self):
+        n = len(self.arrays)
+        arr = (_lib.View * max(n, 1))(*[a.view_struct() for a in self.arrays])
+        return arr, n
+
+    def materialize(self) -> NCDevArray:
+        out = NCDevArray(self.shape, self.expr_dtype)
+        self.evaluate(out=out)
+        return out
+
+    def evaluate(self, out: Optional[NCDevArray] = None, reductions: Iterable = ()):
+        """One fused pass: stores the value into `out` (if given) and computes
+        the reductions, a sequence of (RedOp, axes or None). Returns the list of
+        reduction results (NCDevArray; 0-d for full reductions)."""
+        reductions = list(reductions)
+        t, keep = self._tape()
+        ops, n = self._operands()
+        stream = current_stream()
+        if not reductions:
+            if out is None:
+                raise ValueError("nothing to evaluate")
+            if out.size:
+                _lib.call("nca_expr_eval", ctypes.byref(t), ops, n, ctypes.byref(out.view_struct()), stream)
+            return []
+        shape = out.shape if out is not None else self.shape
+        results, rs = [], []
+        for op, axes in reductions:
+            op = RedOp(op)
+            mask, kept = _axes_mask(axes, len(shape))
+            odt = _red_out_dtype(op, self.expr_dtype)
+            res = NCDevArray([shape[d] for d in kept], odt)
+            results.append(res)
+            r = _lib.Reduction()
+            r.op = int(op)
+            r.axes_mask = mask
+            r.out = res.view_struct()
+            rs.append(r)
+        masks = {r.axes_mask for r in rs}
+        if len(masks) != 1:
+            raise ValueError("one evaluate() call reduces over one set of axes")
+        rarr = (_lib.Reduction * len(rs))(*rs)
+        if out is not None and out.size == 0:
+            out = None
+        _lib.call("nca_expr_reduce", ctypes.byref(t), ops, n,
+                  ctypes.byref(out.view_struct()) if out is not None else None, rarr, len(rs), stream)
+        return results
+
+    def __array__(self, dtype=None, copy=None):
+        return self.materialize().__array__(dtype)
+
+    def to_host(self) -> np.ndarray:
+        return self.materialize().to_host()
+
+    def _reduce(self, op: RedOp, axes):
+        (res,) = self.evaluate(reductions=[(op, axes)])
+        if axes is None:
+            return _scalar(res)
+        return res
+
+    def sum(self, axes=None):
+        return self._reduce(RedOp.SUM, axes)
+
+    def mean(self, axes=None):
+        return self._reduce(RedOp.MEAN, axes)
+
+    def max(self, axes=None):
+        return self._reduce(RedOp.MAX, axes)
+
+    def min(self, axes=None):
+        return self._reduce(RedOp.MIN, axes)
+
+    def argmax(self, axes=None):
+        return self._reduce(RedOp.ARGMAX, axes)
+
+    def argmin(self, axes=None):
+        return self._reduce(RedOp.ARGMIN, axes)
+
+
+def _axes_mask(axes, ndim: int):
+    if axes is None:
+        return (1 << ndim) - 1 if ndim < 32 else 0xFFFFFFFF, []
+    if isinstance(axes, int):
+        axes = [axes]
+    mask = 0
+    for a in axes:
+        a = int(a)
+        if a < 0:
+            a += ndim
+        if not 0 <= a < ndim:
+            raise ValueError("axis out of range")
+        mask |= 1 << a
+    kept = [d for d in range(ndim) if not (mask >> d) & 1]
+    return mask, kept
+
+
+def _red_out_dtype(op: RedOp, dt: DType) -> DType:
+    if op == RedOp.SUM:
+        return sum_type(dt)
+    if op == RedOp.MEAN:
+        return DType.float64
+    if op in (RedOp.MAX, RedOp.MIN):
+        return arith(dt)
+    return DType.int64
+
+
+def _scalar(a: NCDevArray):
+    v = a.to_host().reshape(-1)[0]
+    if a.dtype == DType.bool:
+        return bool(v)
+    if a.dtype in FLOATS:
+        return float(v)
+    return int(v)
+
+
+# ---- operators on arrays and expressions ------------------------------------------
+def _def_ops(cls):
+    binops = {
+        "add": OpCode.ADD, "sub": OpCode.SUB, "mul": OpCode.MUL, "truediv": OpCode.DIV,
+        "mod": OpCode.MOD, "and": OpCode.BAND, "or": OpCode.BOR, "xor": OpCode.XOR,
+    }
+    for name, op in binops.items():
+        def f(self, other, _op=op):
+            return _as_node(self)._binary(_op, other)
+
+        def rf(self, other, _op=op):
+            return _as_node(self)._binary(_op, other, reverse=True)
+        setattr(cls, f"__{name}__", f)
+        setattr(cls, f"__r{name}__", rf)
+    cmps = {"eq": OpCode.EQ, "ne": OpCode.NE, "lt": OpCode.LT, "le": OpCode.LE, "gt": OpCode.GT, "ge": OpCode.GE}
+    for name, op in cmps.items():
+        def c(self, other, _op=op):
+            return _as_node(self)._binary(_op, other)
+        setattr(cls, f"__{name}__", c)
+    cls.__neg__ = lambda self: _as_node(self)._unary(OpCode.NEG)
+    cls.__abs__ = lambda self: _as_node(self)._unary(OpCode.ABS)
+    cls.__invert__ = lambda self: _as_node(self)._unary(OpCode.BNOT)
+    cls.__hash__ = object.__hash__
+
+
+_def_ops(NCDevArray)
+_def_ops(DevExpr)
+
+
+def _inplace(name, op):
+    def f(self, other):
+        with lazy_mode():
+            e = _as_node(self)._binary(op, other)
+        e.evaluate(out=self)
+        return self
+    setattr(NCDevArray, f"__i{name}__", f)
+
+
+for _n, _o in (("add", OpCode.ADD), ("sub", OpCode.SUB), ("mul", OpCode.MUL), ("truediv", OpCode.DIV),
+               ("mod", OpCode.MOD)):
+    _inplace(_n, _o)
+
+
+def sqrt(x):
+    return _as_node(x)._unary(OpCode.SQRT)
+
+
+def absolute(x):
+    return _as_node(x)._unary(OpCode.ABS)
+
+
+def logical_and(a, b):
+    return _as_node(a)._binary(OpCode.LAND, b)
+
+
+def logical_or(a, b):
+    return _as_node(a)._binary(OpCode.LOR, b)
+
+
+def logical_not(a):
+    return _as_node(a)._unary(OpCode.LNOT)
+
+
+def iota(like, dtype: DType = DType.int64):
+    e = DevExpr.iota(like, dtype)
+    return e._finish()

@@ -1,0 +1,1110 @@
+// Expression/reduction engine of libncgb300 (see jit.hpp).
+//
+// Replaces ncarray's device::RuntimeCompiler (src/lib/ncarray/jit/device/
+// rtcompiler.cc:49-510) and the dispatch in GPUEngine::execute_binary_expression,
+// execute_reduce_axes and execute_full_reduce (src/lib/ncarray/engines/
+// gpuengine.hh:90-333). The reference builds one kernel string per tape and
+// launches one thread per element with a div/mod decode per dimension; here a
+// tape is compiled into one of five sm_103a kernel classes chosen from the
+// canonical iteration space (size-1 dims dropped, dims ordered by the output's
+// strides, mergeable dims fused), with 128-bit vector access where the layout
+// allows and reductions fused into the same HBM pass.
+#include "jit.hpp"
+
+#include <nvrtc.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <unordered_map>
+
+namespace nca {
+
+static const char* kPrelude =
+#include "jit_prelude.inc"
+    ;
+static const char* kKernels =
+#include "jit_kernels.inc"
+    ;
+
+// ============================================================================
+// tape validation
+// ============================================================================
+enum Arity { A_NONE = -1, A_LOAD = 0, A_UNARY = 1, A_BINARY = 2 };
+
+static int op_arity(int op) {
+  switch (op) {
+    case NCA_OP_NOOP: return A_NONE;
+    case NCA_OP_IDX: case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR: case NCA_OP_LOAD_CONST:
+      return A_LOAD;
+    case NCA_OP_NEG: case NCA_OP_INC: case NCA_OP_DEC: case NCA_OP_LNOT: case NCA_OP_BNOT:
+    case NCA_OP_ABS: case NCA_OP_SQRT:
+      return A_UNARY;
+    case NCA_OP_ADD: case NCA_OP_SUB: case NCA_OP_MUL: case NCA_OP_DIV: case NCA_OP_MOD:
+    case NCA_OP_EQ: case NCA_OP_NE: case NCA_OP_LT: case NCA_OP_LE: case NCA_OP_GT:
+    case NCA_OP_GE: case NCA_OP_LAND: case NCA_OP_LOR: case NCA_OP_BAND: case NCA_OP_BOR:
+    case NCA_OP_XOR:
+      return A_BINARY;
+    default:
+      return -2;  // SZOF, ADDR, INDR, CAST, FDIV, shifts: not evaluated by the reference VM
+  }
+}
+
+Tape make_tape(const nca_tape* t, int n_operands) {
+  if (!t || !t->instrs) fail(NCA_ERR_INVALID, "null tape");
+  if (t->n_instrs <= 0 || t->n_instrs > NCA_MAX_INSTRS)
+    fail(NCA_ERR_LIMIT, "tape has %d instructions (1..%d)", t->n_instrs, NCA_MAX_INSTRS);
+  if (t->n_scalars < 0 || t->n_scalars > NCA_MAX_SCALARS)
+    fail(NCA_ERR_LIMIT, "tape has %d scalars (0..%d)", t->n_scalars, NCA_MAX_SCALARS);
+  if (t->n_scalars > 0 && (!t->scalar_dtypes || !t->scalar_slots))
+    fail(NCA_ERR_INVALID, "tape scalars missing");
+  Tape r;
+  r.compute_dtype = t->compute_dtype;
+  r.result_dtype = t->result_dtype;
+  if (!dtype_valid(r.compute_dtype) || arith_dtype(r.compute_dtype) != r.compute_dtype)
+    fail(NCA_ERR_DTYPE, "compute dtype %d is not an arithmetic device dtype", r.compute_dtype);
+  if (!dtype_valid(r.result_dtype)) fail(NCA_ERR_DTYPE, "result dtype %d unsupported", r.result_dtype);
+  const bool w_int = !dtinfo(r.compute_dtype).is_float;
+  for (int i = 0; i < t->n_scalars; ++i) {
+    if (!dtype_valid(t->scalar_dtypes[i])) fail(NCA_ERR_DTYPE, "scalar %d dtype %d unsupported", i, t->scalar_dtypes[i]);
+    r.scalar_dtypes.push_back(t->scalar_dtypes[i]);
+    r.scalar_slots.push_back(t->scalar_slots[i]);
+  }
+  int depth = 0;
+  for (int i = 0; i < t->n_instrs; ++i) {
+    const uint32_t ins = t->instrs[i];
+    const int op = (int)(ins >> 24), idx = (int)(ins & 0xffffff);
+    const int ar = op_arity(op);
+    if (ar == -2) fail(NCA_ERR_UNSUPPORTED, "opcode %d is not supported on the device path", op);
+    if ((op == NCA_OP_BNOT || op == NCA_OP_BAND || op == NCA_OP_BOR || op == NCA_OP_XOR) && !w_int)
+      fail(NCA_ERR_DTYPE, "bitwise opcode %d on a floating compute dtype", op);
+    if (op == NCA_OP_LOAD_NCARR || op == NCA_OP_LOAD_SOARR) {
+      if (idx >= n_operands) fail(NCA_ERR_INVALID, "instruction %d loads operand %d of %d", i, idx, n_operands);
+      r.n_arrays = std::max(r.n_arrays, idx + 1);
+    }
+    if (op == NCA_OP_LOAD_CONST && idx >= t->n_scalars)
+      fail(NCA_ERR_INVALID, "instruction %d loads scalar %d of %d", i, idx, t->n_scalars);
+    if (op == NCA_OP_IDX) r.uses_idx = true;
+    if (ar == A_LOAD) ++depth;
+    else if (ar == A_UNARY) { if (depth < 1) fail(NCA_ERR_INVALID, "stack underflow at %d", i); }
+    else if (ar == A_BINARY) { if (depth < 2) fail(NCA_ERR_INVALID, "stack underflow at %d", i); --depth; }
+    if (depth > 64) fail(NCA_ERR_LIMIT, "tape stack deeper than 64");
+    r.instrs.push_back(ins);
+  }
+  if (depth != 1) fail(NCA_ERR_INVALID, "tape leaves %d values on the stack (expected 1)", depth);
+  return r;
+}
+
+// ============================================================================
+// host-side scalar conversion (static_cast<W>(scalar), op_traits::cast)
+// ============================================================================
+template <class To, class From>
+static To hcast(From v) { return static_cast<To>(v); }
+
+static float bf16_to_f32_host(uint16_t h) { uint32_t u = (uint32_t)h << 16; float f; memcpy(&f, &u, 4); return f; }
+static float f16_to_f32_host(uint16_t h) {
+  const uint32_t s = (h >> 15) & 1u, e = (h >> 10) & 0x1fu, m = h & 0x3ffu;
+  float f;
+  if (e == 0) f = (float)m * (1.0f / 16777216.0f);  // m * 2^-24
+  else if (e == 31) { uint32_t u = (s << 31) | 0x7f800000u | (m << 13); memcpy(&f, &u, 4); return f; }
+  else { uint32_t u = (s << 31) | ((e + 112u) << 23) | (m << 13); memcpy(&f, &u, 4); return f; }
+  return s ? -f : f;
+}
+
+template <class W>
+static W scalar_as(int sd, uint64_t slot) {
+  switch (sd) {
+    case NCA_BOOL: return hcast<W>((uint8_t)(slot & 0xff) != 0);
+    case NCA_CHAR: case NCA_INT8: return hcast<W>((int8_t)(slot & 0xff));
+    case NCA_UINT8: return hcast<W>((uint8_t)(slot & 0xff));
+    case NCA_UINT16: return hcast<W>((uint16_t)(slot & 0xffff));
+    case NCA_INT16: return hcast<W>((int16_t)(slot & 0xffff));
+    case NCA_UINT32: return hcast<W>((uint32_t)slot);
+    case NCA_INT32: return hcast<W>((int32_t)(uint32_t)slot);
+    case NCA_UINT64: return hcast<W>((uint64_t)slot);
+    case NCA_INT64: return hcast<W>((int64_t)slot);
+    case NCA_FLOAT32: { uint32_t u = (uint32_t)slot; float f; memcpy(&f, &u, 4); return hcast<W>(f); }
+    case NCA_FLOAT64: { double d; memcpy(&d, &slot, 8); return hcast<W>(d); }
+    case NCA_BFLOAT16: return hcast<W>(bf16_to_f32_host((uint16_t)slot));
+    case NCA_FLOAT16: return hcast<W>(f16_to_f32_host((uint16_t)slot));
+  }
+  fail(NCA_ERR_DTYPE, "bad scalar dtype %d", sd);
+}
+
+template <class W>
+static uint64_t bits_of(W v) { uint64_t r = 0; memcpy(&r, &v, sizeof(W)); return r; }
+
+static uint64_t scalar_word(int wdt, int sd, uint64_t slot) {
+  switch (wdt) {
+    case NCA_BOOL: return bits_of<bool>(scalar_as<bool>(sd, slot));
+    case NCA_CHAR: case NCA_INT8: return bits_of<int8_t>(scalar_as<int8_t>(sd, slot));
+    case NCA_UINT8: return bits_of<uint8_t>(scalar_as<uint8_t>(sd, slot));
+    case NCA_UINT16: return bits_of<uint16_t>(scalar_as<uint16_t>(sd, slot));
+    case NCA_INT16: return bits_of<int16_t>(scalar_as<int16_t>(sd, slot));
+    case NCA_UINT32: return bits_of<uint32_t>(scalar_as<uint32_t>(sd, slot));
+    case NCA_INT32: return bits_of<int32_t>(scalar_as<int32_t>(sd, slot));
+    case NCA_UINT64: return bits_of<uint64_t>(scalar_as<uint64_t>(sd, slot));
+    case NCA_INT64: return bits_of<int64_t>(scalar_as<int64_t>(sd, slot));
+    case NCA_FLOAT32: return bits_of<float>(scalar_as<float>(sd, slot));
+    case NCA_FLOAT64: return bits_of<double>(scalar_as<double>(sd, slot));
+  }
+  fail(NCA_ERR_DTYPE, "bad compute dtype %d", wdt);
+}
+
+// ============================================================================
+// canonical iteration space
+// ============================================================================
+struct CArr {
+  const char* base = nullptr;
+  int dtype = 0;
+  int64_t st[NCA_MAX_NDIM] = {0};
+};
+
+struct Space {
+  int nd = 0;
+  int64_t shape[NCA_MAX_NDIM] = {0};
+  bool red[NCA_MAX_NDIM] = {false};
+  std::vector<CArr> ops;
+  bool has_out = false;
+  CArr out;
+  std::vector<CArr> reds;
+  int64_t total() const { int64_t t = 1; for (int d = 0; d < nd; ++d) t *= shape[d]; return t; }
+};
+
+static void check_view(const nca_view& v, const char* what) {
+  if (v.ndim < 0 || v.ndim > NCA_MAX_NDIM) fail(NCA_ERR_LIMIT, "%s: ndim %d (0..%d)", what, v.ndim, NCA_MAX_NDIM);
+  if (!dtype_valid(v.dtype)) fail(NCA_ERR_DTYPE, "%s: dtype %d not supported on the device", what, v.dtype);
+  if (v.pointer_axis >= 0) fail(NCA_ERR_UNSUPPORTED, "%s: pointer axes are not supported on the device path", what);
+  if (v.flags != 0) fail(NCA_ERR_INVALID, "%s: flags must be 0", what);
+  int64_t n = 1;
+  for (int d = 0; d < v.ndim; ++d) {
+    if (v.shape[d] < 0) fail(NCA_ERR_SHAPE, "%s: negative extent", what);
+    n *= v.shape[d];
+  }
+  if (n > 0 && !v.data) fail(NCA_ERR_INVALID, "%s: null data pointer", what);
+}
+
+static const char* view_base(const nca_view& v) {
+  int64_t off = 0;
+  for (int d = 0; d < v.ndim; ++d) off += v.offsets[d];
+  return static_cast<const char*>(v.data) + off;
+}
+
+// Builds the logical-order space (size-1 dims dropped). `lshape` has n dims.
+static Space make_space(const int64_t* lshape, int n, const nca_view* ops, int nops,
+                        const nca_view* out, uint32_t red_mask, const nca_reduction* reds, int nred) {
+  Space s;
+  for (int k = 0; k < nops; ++k) {
+    CArr a; a.base = view_base(ops[k]); a.dtype = ops[k].dtype; s.ops.push_back(a);
+  }
+  if (out) { s.has_out = true; s.out.base = view_base(*out); s.out.dtype = out->dtype; }
+  for (int k = 0; k < nred; ++k) {
+    CArr a; a.base = view_base(reds[k].out); a.dtype = reds[k].out.dtype; s.reds.push_back(a);
+  }
+  int kept_pos = 0;
+  for (int d = 0; d < n; ++d) {
+    const bool is_red = (red_mask >> d) & 1u;
+    const int kd = kept_pos;
+    if (!is_red) ++kept_pos;
+    if (lshape[d] == 1) continue;
+    const int c = s.nd++;
+    s.shape[c] = lshape[d];
+    s.red[c] = is_red;
+    for (int k = 0; k < nops; ++k) {
+      const nca_view& v = ops[k];
+      const int vd = d - (n - v.ndim);
+      s.ops[k].st[c] = (vd >= 0 && v.shape[vd] != 1) ? v.strides[vd] : 0;
+    }
+    if (out) s.out.st[c] = out->strides[d];
+    for (int k = 0; k < nred; ++k) s.reds[k].st[c] = is_red ? 0 : reds[k].out.strides[kd];
+  }
+  return s;
+}
+
+static bool mergeable(const Space& s, int i) {  // dims i (outer) and i+1 (inner)
+  if (s.red[i] != s.red[i + 1]) return false;
+  auto ok = [&](const CArr& a) { return a.st[i] == a.st[i + 1] * s.shape[i + 1]; };
+  for (auto& a : s.ops) if (!ok(a)) return false;
+  if (s.has_out && !ok(s.out)) return false;
+  for (auto& a : s.reds) if (!ok(a)) return false;
+  return true;
+}
+
+static void merge_dims(Space& s) {
+  for (int i = s.nd - 2; i >= 0; --i) {
+    if (!mergeable(s, i)) continue;
+    s.shape[i] *= s.shape[i + 1];
+    auto fold = [&](CArr& a) {
+      a.st[i] = a.st[i + 1];
+      for (int d = i + 1; d + 1 < s.nd; ++d) a.st[d] = a.st[d + 1];
+    };
+    for (auto& a : s.ops) fold(a);
+    if (s.has_out) fold(s.out);
+    for (auto& a : s.reds) fold(a);
+    for (int d = i + 1; d + 1 < s.nd; ++d) { s.shape[d] = s.shape[d + 1]; s.red[d] = s.red[d + 1]; }
+    --s.nd;
+  }
+}
+
+static void permute_dims(Space& s, const std::vector<int>& perm) {
+  Space t = s;
+  for (int c = 0; c < s.nd; ++c) {
+    t.shape[c] = s.shape[perm[c]];
+    t.red[c] = s.red[perm[c]];
+    for (size_t k = 0; k < s.ops.size(); ++k) t.ops[k].st[c] = s.ops[k].st[perm[c]];
+    if (s.has_out) t.out.st[c] = s.out.st[perm[c]];
+    for (size_t k = 0; k < s.reds.size(); ++k) t.reds[k].st[c] = s.reds[k].st[perm[c]];
+  }
+  s = t;
+}
+
+static void ensure_nd1(Space& s) {
+  if (s.nd > 0) return;
+  s.nd = 1;
+  s.shape[0] = 1;
+  s.red[0] = false;
+}
+
+// ============================================================================
+// source generation
+// ============================================================================
+enum { M_CONTIG = 0, M_CONST = 1, M_STRIDED = 2 };
+
+struct Spec {
+  int kind = 1, nops = 0, nd = 1, vec = 1, idx32 = 0, nkept = 0, team = 256;
+  uint32_t kept_mask = 0;
+  bool has_out = false;
+  int out_dtype = NCA_FLOAT64, w = NCA_FLOAT64, r = NCA_FLOAT64;
+  int nred = 0;
+  uint32_t red_ops = 0;
+  bool has_sum = false, has_max = false, has_min = false;
+  std::vector<int> op_dtypes, op_modes;
+  int nscal = 0;
+};
+
+struct WordLayout {
+  int opb, ops, outb, outs, shape, scal, redb, reds, total, psum, pmax, pmin, nsplit, chunk,
+      keptn, redn, magic, nwords;
+};
+
+static WordLayout word_layout(int nops, int nd, int nscal, int nred) {
+  WordLayout L;
+  int p = 0;
+  L.opb = p; p += nops;
+  L.ops = p; p += nops * nd;
+  L.outb = p; p += 1;
+  L.outs = p; p += nd;
+  L.shape = p; p += nd;
+  L.scal = p; p += nscal;
+  L.redb = p; p += nred;
+  L.reds = p; p += nred * nd;
+  L.total = p++; L.psum = p++; L.pmax = p++; L.pmin = p++; L.nsplit = p++; L.chunk = p++;
+  L.keptn = p++; L.redn = p++;
+  L.magic = p; p += nd;
+  L.nwords = p;
+  return L;
+}
+
+static std::string cty(int dt) {  // arithmetic C type of a dtype (16-bit floats -> float)
+  return arith_dtype(dt) == NCA_FLOAT32 && dt != NCA_FLOAT32 ? "float" : dtinfo(dt).ctype;
+}
+
+// value of a dtype from raw bits held in an integer expression
+static std::string from_bits(int dt, const std::string& b) {
+  switch (dt) {
+    case NCA_BOOL: return "((((u32)(" + b + ")) & 0xffu) != 0u)";
+    case NCA_CHAR: case NCA_INT8: return "((signed char)(unsigned char)(" + b + "))";
+    case NCA_UINT8: return "((unsigned char)(" + b + "))";
+    case NCA_INT16: return "((short)(unsigned short)(" + b + "))";
+    case NCA_UINT16: return "((unsigned short)(" + b + "))";
+    case NCA_INT32: return "((int)(u32)(" + b + "))";
+    case NCA_UINT32: return "((u32)(" + b + "))";
+    case NCA_INT64: return "((i64)(" + b + "))";
+    case NCA_UINT64: return "((u64)(" + b + "))";
+    case NCA_FLOAT32: return "__uint_as_float((u32)(" + b + "))";
+    case NCA_FLOAT64: return "__longlong_as_double((i64)(" + b + "))";
+    case NCA_BFLOAT16: return "nca_bf16_to_f32((unsigned short)(" + b + "))";
+    case NCA_FLOAT16: return "nca_f16_to_f32((unsigned short)(" + b + "))";
+  }
+  fail(NCA_ERR_DTYPE, "from_bits dtype %d", dt);
+}
+
+// raw bits (u32 for <=4 bytes, u64 for 8) of value expression v stored as dtype dt
+static std::string to_bits(int dt, const std::string& v) {
+  switch (dt) {
+    case NCA_BOOL: return "((u32)((" + v + ") != 0))";
+    case NCA_CHAR: case NCA_INT8: return "((u32)(unsigned char)(signed char)(" + v + "))";
+    case NCA_UINT8: return "((u32)(unsigned char)(" + v + "))";
+    case NCA_INT16: return "((u32)(unsigned short)(short)(" + v + "))";
+    case NCA_UINT16: return "((u32)(unsigned short)(" + v + "))";
+    case NCA_INT32: return "((u32)(int)(" + v + "))";
+    case NCA_UINT32: return "((u32)(" + v + "))";
+    case NCA_INT64: return "((u64)(i64)(" + v + "))";
+    case NCA_UINT64: return "((u64)(" + v + "))";
+    case NCA_FLOAT32: return "((u32)__float_as_uint((float)(" + v + ")))";
+    case NCA_FLOAT64: return "((u64)__double_as_longlong((double)(" + v + ")))";
+    case NCA_BFLOAT16: return "((u32)nca_f32_to_bf16((float)(" + v + ")))";
+    case NCA_FLOAT16: return "((u32)nca_f32_to_f16((float)(" + v + ")))";
+  }
+  fail(NCA_ERR_DTYPE, "to_bits dtype %d", dt);
+}
+
+static std::string storage_uint(int size) {
+  switch (size) { case 1: return "unsigned char"; case 2: return "unsigned short"; case 4: return "u32"; default: return "u64"; }
+}
+
+static const char* kWordNames[4] = {"x", "y", "z", "w"};
+
+// expression of lane q's bits in a vector of `bytes` loaded into variable u
+static std::string lane_bits(int bytes, int es, int q, const std::string& u) {
+  auto word = [&](int i) -> std::string {
+    if (bytes == 16 || bytes == 8) return u + "." + kWordNames[i];
+    return u;
+  };
+  if (es == 8) return "((((u64)" + word(2 * q + 1) + ") << 32) | (u64)" + word(2 * q) + ")";
+  if (es == 4) return word(q);
+  if (bytes <= 4 && es * 1 == bytes) return "(u32)" + u;
+  const int bo = q * es;
+  const int wi = bytes >= 8 ? bo / 4 : 0;
+  const int sh = (bytes >= 8 ? bo % 4 : bo) * 8;
+  return "((((u32)" + word(wi) + ") >> " + std::to_string(sh) + ") & " + (es == 1 ? "0xffu" : "0xffffu") + ")";
+}
+
+static std::string vec_type(int bytes) {
+  switch (bytes) { case 16: return "uint4"; case 8: return "uint2"; case 4: return "u32"; case 2: return "unsigned short"; default: return "unsigned char"; }
+}
+
+static std::string gen_eval(const Tape& t) {
+  std::ostringstream os;
+  std::vector<std::string> st;
+  int tmp = 0;
+  const std::string W = "nca_w";
+  for (uint32_t ins : t.instrs) {
+    const int op = (int)(ins >> 24), idx = (int)(ins & 0xffffff);
+    auto push_tmp = [&](const std::string& e) {
+      const std::string n = "t" + std::to_string(tmp++);
+      os << "  const nca_w " << n << " = " << e << ";\n";
+      st.push_back(n);
+    };
+    switch (op) {
+      case NCA_OP_NOOP: break;
+      case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR: st.push_back("v[" + std::to_string(idx) + "][q]"); break;
+      case NCA_OP_LOAD_CONST: st.push_back("s[" + std::to_string(idx) + "]"); break;
+      case NCA_OP_IDX: push_tmp("(nca_w)lin"); break;
+      default: {
+        const int ar = op_arity(op);
+        if (ar == A_UNARY) {
+          const std::string a = st.back(); st.pop_back();
+          const char* f = op == NCA_OP_NEG ? "nca_neg" : op == NCA_OP_INC ? "nca_inc" : op == NCA_OP_DEC ? "nca_dec"
+                        : op == NCA_OP_LNOT ? "nca_lnot" : op == NCA_OP_BNOT ? "nca_bnot" : op == NCA_OP_ABS ? "nca_abs" : "nca_sqrt";
+          push_tmp(std::string(f) + "<nca_w>(" + a + ")");
+        } else {
+          const std::string b = st.back(); st.pop_back();
+          const std::string a = st.back(); st.pop_back();
+          const char* f = nullptr;
+          switch (op) {
+            case NCA_OP_ADD: f = "nca_add"; break; case NCA_OP_SUB: f = "nca_sub"; break;
+            case NCA_OP_MUL: f = "nca_mul"; break; case NCA_OP_DIV: f = "nca_div"; break;
+            case NCA_OP_MOD: f = "nca_mod"; break; case NCA_OP_EQ: f = "nca_eq"; break;
+            case NCA_OP_NE: f = "nca_ne"; break; case NCA_OP_LT: f = "nca_lt"; break;
+            case NCA_OP_LE: f = "nca_le"; break; case NCA_OP_GT: f = "nca_gt"; break;
+            case NCA_OP_GE: f = "nca_ge"; break; case NCA_OP_LAND: f = "nca_land"; break;
+            case NCA_OP_LOR: f = "nca_lor"; break; case NCA_OP_BAND: f = "nca_band"; break;
+            case NCA_OP_BOR: f = "nca_bor"; break; case NCA_OP_XOR: f = "nca_xor"; break;
+            default: fail(NCA_ERR_UNSUPPORTED, "opcode %d", op);
+          }
+          push_tmp(std::string(f) + "<nca_w>(" + a + ", " + b + ")");
+        }
+      }
+    }
+  }
+  std::string res = st.back();
+  return os.str() + "  return " + res + ";\n";
+}
+
+static std::string lim_expr(int dt, bool lowest) {
+  switch (arith_dtype(dt)) {
+    case NCA_BOOL: return lowest ? "false" : "true";
+    case NCA_CHAR: case NCA_INT8: return lowest ? "((signed char)-128)" : "((signed char)127)";
+    case NCA_UINT8: return lowest ? "((unsigned char)0)" : "((unsigned char)255)";
+    case NCA_INT16: return lowest ? "((short)-32768)" : "((short)32767)";
+    case NCA_UINT16: return lowest ? "((unsigned short)0)" : "((unsigned short)65535)";
+    case NCA_INT32: return lowest ? "((int)0x80000000)" : "((int)0x7fffffff)";
+    case NCA_UINT32: return lowest ? "0u" : "0xffffffffu";
+    case NCA_INT64: return lowest ? "((i64)0x8000000000000000ull)" : "((i64)0x7fffffffffffffffll)";
+    case NCA_UINT64: return lowest ? "0ull" : "0xffffffffffffffffull";
+    case NCA_FLOAT32: return lowest ? "__uint_as_float(0xff7fffffu)" : "__uint_as_float(0x7f7fffffu)";
+    case NCA_FLOAT64: return lowest ? "__longlong_as_double((i64)0xffefffffffffffffull)" : "__longlong_as_double(0x7fefffffffffffffll)";
+  }
+  fail(NCA_ERR_DTYPE, "limits of dtype %d", dt);
+}
+
+static std::string gen_source(const Spec& sp, const Tape& t) {
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  std::ostringstream os;
+  os << kPrelude;
+  os << "#define NCA_NOPS " << sp.nops << "\n#define NCA_ND " << sp.nd << "\n#define NCA_NRED " << sp.nred
+     << "\n#define NCA_KIND " << sp.kind << "\n#define NCA_VEC " << sp.vec << "\n#define NCA_IDX32 " << sp.idx32
+     << "\n#define NCA_NKEPT " << sp.nkept << "\n#define NCA_KEPT_MASK " << sp.kept_mask << "u"
+     << "\n#define NCA_RED_OPS " << sp.red_ops << "u\n#define NCA_TEAM " << sp.team
+     << "\n#define NCA_HAS_OUT " << (sp.has_out ? 1 : 0) << "\n#define NCA_NWORDS " << L.nwords
+     << "\n#define NCA_HAS_SUM " << (sp.has_sum ? 1 : 0) << "\n#define NCA_HAS_MAX " << (sp.has_max ? 1 : 0)
+     << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n";
+  int sum_mode = 1;
+  if (sp.nred > 0) {
+    const int ra = arith_dtype(sp.r);
+    sum_mode = ra == NCA_FLOAT32 ? 0 : ra == NCA_FLOAT64 ? 1 : 2;
+  }
+  os << "#define NCA_SUM_MODE " << sum_mode << "\n";
+  os << "#define NCA_W_OPB " << L.opb << "\n#define NCA_W_OPS " << L.ops << "\n#define NCA_W_OUTB " << L.outb
+     << "\n#define NCA_W_OUTS " << L.outs << "\n#define NCA_W_SHAPE " << L.shape << "\n#define NCA_W_SCAL " << L.scal
+     << "\n#define NCA_W_REDB " << L.redb << "\n#define NCA_W_REDS " << L.reds << "\n#define NCA_W_TOTAL " << L.total
+     << "\n#define NCA_W_PSUM " << L.psum << "\n#define NCA_W_PMAX " << L.pmax << "\n#define NCA_W_PMIN " << L.pmin
+     << "\n#define NCA_W_NSPLIT " << L.nsplit << "\n#define NCA_W_CHUNK " << L.chunk << "\n#define NCA_W_KEPTN " << L.keptn
+     << "\n#define NCA_W_REDN " << L.redn << "\n#define NCA_W_MAGIC " << L.magic << "\n";
+  os << "typedef " << dtinfo(sp.w).ctype << " nca_w;\n";
+  const std::string rty = sp.nred > 0 ? cty(sp.r) : std::string("nca_w");
+  os << "typedef " << rty << " nca_r;\n";
+  os << "#define NCA_R_LOWEST " << (sp.nred > 0 ? lim_expr(sp.r, true) : "0") << "\n";
+  os << "#define NCA_R_HIGHEST " << (sp.nred > 0 ? lim_expr(sp.r, false) : "0") << "\n";
+  os << "struct NcaArgs;\n";
+
+  // ---- loads: nca_gather (NCA_VEC lanes) and nca_gather1 (lane 0, scalar) ----
+  os << "#define OPB_(k) ((const char*)A.w[" << L.opb << " + (k)])\n";
+  os << "#define OPS_(k, d) ((i64)A.w[" << L.ops << " + (k) * " << sp.nd << " + (d)])\n";
+  auto scalar_load = [&](int k, const std::string& ptr) {
+    const int dt = sp.op_dtypes[k];
+    const int sz = dtinfo(dt).size;
+    return "(nca_w)(" + from_bits(dt, "*(const " + storage_uint(sz) + "*)(" + ptr + ")") + ")";
+  };
+  std::ostringstream g, g1;
+  for (int k = 0; k < sp.nops; ++k) {
+    const int dt = sp.op_dtypes[k];
+    const int es = dtinfo(dt).size;
+    const std::string base = "OPB_(" + std::to_string(k) + ") + off[" + std::to_string(k) + "]";
+    g1 << "  v[" << k << "][0] = " << scalar_load(k, base) << ";\n";
+    const int mode = sp.op_modes[k];
+    if (mode == M_CONST || sp.vec == 1) {
+      g << "  { const nca_w x = " << scalar_load(k, base) << ";";
+      for (int q = 0; q < sp.vec; ++q) g << " v[" << k << "][" << q << "] = x;";
+      g << " }\n";
+    } else if (mode == M_CONTIG) {
+      const int bytes = es * sp.vec;
+      g << "  { const " << vec_type(bytes) << " u = *(const " << vec_type(bytes) << "*)(" << base << ");";
+      for (int q = 0; q < sp.vec; ++q)
+        g << " v[" << k << "][" << q << "] = (nca_w)(" << from_bits(dt, lane_bits(bytes, es, q, "u")) << ");";
+      g << " }\n";
+    } else {
+      for (int q = 0; q < sp.vec; ++q)
+        g << "  v[" << k << "][" << q << "] = "
+          << scalar_load(k, base + " + " + std::to_string(q) + " * OPS_(" + std::to_string(k) + ", " + std::to_string(sp.nd - 1) + ")")
+          << ";\n";
+    }
+  }
+  // the kernels take `const NcaArgs A`; the helpers take it by reference
+  os << "struct NcaArgs { u64 w[" << L.nwords << "]; };\n";
+  os << "__device__ __forceinline__ void nca_gather(const NcaArgs& A, const i64* off, nca_w (*v)[NCA_VEC]) {\n"
+     << g.str() << "}\n";
+  os << "__device__ __forceinline__ void nca_gather1(const NcaArgs& A, const i64* off, nca_w (*v)[NCA_VEC]) {\n"
+     << g1.str() << "}\n";
+  os << "__device__ __forceinline__ nca_w nca_eval(const nca_w (*v)[NCA_VEC], int q, const nca_w* s, i64 lin) {\n"
+     << "  (void)v; (void)q; (void)s; (void)lin;\n"
+     << gen_eval(t) << "}\n";
+
+  // ---- stores ----
+  if (sp.has_out) {
+    const int dt = sp.out_dtype;
+    const int es = dtinfo(dt).size;
+    os << "__device__ __forceinline__ void nca_put1(char* p, nca_w e) { *(" << storage_uint(es) << "*)p = ("
+       << storage_uint(es) << ")" << to_bits(dt, "e") << "; }\n";
+    os << "__device__ __forceinline__ void nca_put(char* p, const nca_w* e) {\n";
+    const int bytes = es * sp.vec;
+    if (sp.vec == 1) {
+      os << "  nca_put1(p, e[0]);\n";
+    } else if (es == 8) {
+      os << "  " << vec_type(bytes) << " u;\n";
+      for (int q = 0; q < sp.vec; ++q) {
+        os << "  { const u64 b = " << to_bits(dt, "e[" + std::to_string(q) + "]") << "; u." << kWordNames[2 * q]
+           << " = (u32)b; u." << kWordNames[2 * q + 1] << " = (u32)(b >> 32); }\n";
+      }
+      os << "  *(" << vec_type(bytes) << "*)p = u;\n";
+    } else if (es == 4) {
+      os << "  " << vec_type(bytes) << " u;\n";
+      for (int q = 0; q < sp.vec; ++q) {
+        if (bytes == 4) os << "  u = " << to_bits(dt, "e[0]") << ";\n";
+        else os << "  u." << kWordNames[q] << " = " << to_bits(dt, "e[" + std::to_string(q) + "]") << ";\n";
+      }
+      os << "  *(" << vec_type(bytes) << "*)p = u;\n";
+    } else {
+      const int nwords = bytes >= 4 ? bytes / 4 : 1;
+      const int per = bytes >= 4 ? 4 / es : sp.vec;
+      for (int wi = 0; wi < nwords; ++wi) {
+        os << "  u32 w" << wi << " = 0u;\n";
+        for (int j = 0; j < per; ++j) {
+          const int q = wi * per + j;
+          os << "  w" << wi << " |= (" << to_bits(dt, "e[" + std::to_string(q) + "]") << ") << " << (j * es * 8) << ";\n";
+        }
+      }
+      if (bytes >= 8) {
+        os << "  " << vec_type(bytes) << " u;";
+        for (int wi = 0; wi < nwords; ++wi) os << " u." << kWordNames[wi] << " = w" << wi << ";";
+        os << "\n  *(" << vec_type(bytes) << "*)p = u;\n";
+      } else {
+        os << "  *(" << vec_type(bytes) << "*)p = (" << vec_type(bytes) << ")w0;\n";
+      }
+    }
+    os << "}\n";
+  }
+  // ---- reductions ----
+  if (sp.nred > 0) {
+    if (sp.r == NCA_BFLOAT16) os << "__device__ __forceinline__ nca_r nca_to_r(nca_w e) { return nca_bf16_to_f32(nca_f32_to_bf16((float)e)); }\n";
+    else if (sp.r == NCA_FLOAT16) os << "__device__ __forceinline__ nca_r nca_to_r(nca_w e) { return nca_f16_to_f32(nca_f32_to_f16((float)e)); }\n";
+    else if (sp.r == NCA_BOOL) os << "__device__ __forceinline__ nca_r nca_to_r(nca_w e) { return e != 0; }\n";
+    else os << "__device__ __forceinline__ nca_r nca_to_r(nca_w e) { return (nca_r)e; }\n";
+    const int sdt = sum_dtype(sp.r);
+    const bool sgn = dtinfo(arith_dtype(sp.r)).is_signed;
+    if (sum_mode == 2) {
+      os << "__device__ __forceinline__ void nca_store_sum(char* p, u64 s) { *(" << storage_uint(dtinfo(sdt).size)
+         << "*)p = (" << storage_uint(dtinfo(sdt).size) << ")s; }\n";
+      os << "__device__ __forceinline__ double nca_sum_as_double(u64 s) { return (double)(" << (sgn ? "(i64)s" : "s") << "); }\n";
+    } else {
+      if (sdt == NCA_FLOAT32) os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(float*)p = __double2float_rn(s); }\n";
+      else os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(double*)p = s; }\n";
+      os << "__device__ __forceinline__ double nca_sum_as_double(double s) { return s; }\n";
+    }
+  }
+  os << "#undef OPB_\n#undef OPS_\n";
+  // the template redefines NcaArgs; skip that line by guarding
+  std::string body = kKernels;
+  const std::string decl = "struct NcaArgs { u64 w[NCA_NWORDS]; };";
+  const size_t pos = body.find(decl);
+  if (pos != std::string::npos) body.erase(pos, decl.size());
+  os << body;
+  return os.str();
+}
+
+// ============================================================================
+// NVRTC + cache
+// ============================================================================
+static uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
+  for (unsigned char c : s) { h ^= c; h *= 1099511628211ull; }
+  return h;
+}
+
+struct JitState {
+  std::mutex m;
+  std::unordered_map<std::string, std::vector<char>> cubins;                 // key -> cubin
+  std::map<std::pair<std::string, int>, CUfunction> funcs;                   // (key, device) -> fn
+  std::string cache_dir;
+  bool cache_dir_set = false;
+  std::atomic<int64_t> compiled{0}, disk_hits{0}, mem_hits{0};
+};
+
+static JitState& js() { static JitState s; return s; }
+
+static std::string default_cache_dir() {
+  if (const char* e = getenv("NCA_GB300_CACHE_DIR")) if (*e) return e;
+  if (const char* x = getenv("XDG_CACHE_HOME")) if (*x) return std::string(x) + "/ncarray_gb300";
+  if (const char* h = getenv("HOME")) if (*h) return std::string(h) + "/.cache/ncarray_gb300";
+  return "/tmp/ncarray_gb300";
+}
+
+std::string jit_cache_dir() {
+  auto& s = js();
+  std::lock_guard<std::mutex> lk(s.m);
+  if (!s.cache_dir_set) { s.cache_dir = default_cache_dir(); s.cache_dir_set = true; }
+  return s.cache_dir;
+}
+
+void jit_set_cache_dir(const char* dir) {
+  auto& s = js();
+  std::lock_guard<std::mutex> lk(s.m);
+  s.cache_dir = dir ? std::string(dir) : default_cache_dir();
+  s.cache_dir_set = true;
+}
+
+void jit_stats(int64_t* c, int64_t* d, int64_t* m) {
+  auto& s = js();
+  if (c) *c = s.compiled.load();
+  if (d) *d = s.disk_hits.load();
+  if (m) *m = s.mem_hits.load();
+}
+
+static void mkdirs(const std::string& path) {
+  std::string cur;
+  for (size_t i = 0; i < path.size(); ++i) {
+    cur += path[i];
+    if (path[i] == '/' && cur.size() > 1) mkdir(cur.c_str(), 0755);
+  }
+  mkdir(path.c_str(), 0755);
+}
+
+static const char kMagic[8] = {'N', 'C', 'A', 'J', 'I', 'T', '1', 0};
+
+static bool disk_load(const std::string& file, std::vector<char>& out) {
+  std::ifstream f(file, std::ios::binary);
+  if (!f) return false;
+  char magic[8];
+  uint64_t len = 0, h = 0;
+  if (!f.read(magic, 8) || memcmp(magic, kMagic, 8) != 0) return false;
+  if (!f.read(reinterpret_cast<char*>(&len), 8) || len == 0 || len > (64ull << 20)) return false;
+  out.resize(len);
+  if (!f.read(out.data(), (std::streamsize)len)) return false;
+  if (!f.read(reinterpret_cast<char*>(&h), 8)) return false;
+  return h == fnv1a(std::string(out.data(), out.size()));
+}
+
+static void disk_store(const std::string& dir, const std::string& file, const std::vector<char>& cubin) {
+  mkdirs(dir);
+  const std::string tmp = file + ".tmp." + std::to_string((long)getpid());
+  {
+    std::ofstream f(tmp, std::ios::binary);
+    if (!f) return;
+    const uint64_t len = cubin.size(), h = fnv1a(std::string(cubin.data(), cubin.size()));
+    f.write(kMagic, 8);
+    f.write(reinterpret_cast<const char*>(&len), 8);
+    f.write(cubin.data(), (std::streamsize)len);
+    f.write(reinterpret_cast<const char*>(&h), 8);
+    if (!f) { std::remove(tmp.c_str()); return; }
+  }
+  std::rename(tmp.c_str(), file.c_str());
+}
+
+static std::string arch_for(int dev) {
+  int major = 0, minor = 0;
+  check_cuda(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev), "cc major");
+  check_cuda(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev), "cc minor");
+  std::string a = "sm_" + std::to_string(major) + std::to_string(minor);
+  if (major >= 9) a += "a";
+  return a;
+}
+
+static std::vector<char> nvrtc_compile(const std::string& src, const std::string& arch) {
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "nca_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+    fail(NCA_ERR_COMPILE, "nvrtcCreateProgram failed");
+  const std::string archopt = "--gpu-architecture=" + arch;
+  const char* opts[] = {archopt.c_str(), "--fmad=false", "--std=c++17", "-DNDEBUG", "-lineinfo"};
+  nvrtcResult r = nvrtcCompileProgram(prog, 5, opts);
+  if (r != NVRTC_SUCCESS) {
+    size_t n = 0;
+    nvrtcGetProgramLogSize(prog, &n);
+    std::string log(n, '\0');
+    if (n) nvrtcGetProgramLog(prog, &log[0]);
+    nvrtcDestroyProgram(&prog);
+    if (log.size() > 3000) log = log.substr(0, 3000);
+    fail(NCA_ERR_COMPILE, "NVRTC: %s\n%s", nvrtcGetErrorString(r), log.c_str());
+  }
+  size_t n = 0;
+  nvrtcGetCUBINSize(prog, &n);
+  std::vector<char> cubin(n);
+  nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  return cubin;
+}
+
+static std::string nvrtc_version_tag() {
+  int a = 0, b = 0;
+  nvrtcVersion(&a, &b);
+  return std::to_string(a) + "." + std::to_string(b);
+}
+
+CUfunction jit_get(const std::string& source, const char* name) {
+  const int dev = current_device();
+  const std::string arch = arch_for(dev);
+  const std::string key = [&] {
+    char buf[32];
+    snprintf(buf, sizeof(buf), "%016llx", (unsigned long long)fnv1a(source + "|" + arch + "|" + nvrtc_version_tag() + "|" + name + "|fmad=false"));
+    return std::string(buf) + "_" + arch;
+  }();
+  auto& s = js();
+  {
+    std::lock_guard<std::mutex> lk(s.m);
+    auto it = s.funcs.find({key, dev});
+    if (it != s.funcs.end()) { s.mem_hits++; return it->second; }
+  }
+  std::vector<char> cubin;
+  bool have = false;
+  {
+    std::lock_guard<std::mutex> lk(s.m);
+    auto it = s.cubins.find(key);
+    if (it != s.cubins.end()) { cubin = it->second; have = true; }
+  }
+  const std::string dir = jit_cache_dir();
+  const std::string file = dir + "/" + key + ".cubin";
+  if (!have && disk_load(file, cubin)) { have = true; s.disk_hits++; }
+  if (!have) {
+    cubin = nvrtc_compile(source, arch);
+    s.compiled++;
+    disk_store(dir, file, cubin);
+  }
+  CUmodule mod;
+  check_cu(drv().cuModuleLoadData(&mod, cubin.data()), "cuModuleLoadData");
+  CUfunction fn;
+  check_cu(drv().cuModuleGetFunction(&fn, mod, name), "cuModuleGetFunction");
+  std::lock_guard<std::mutex> lk(s.m);
+  s.cubins[key] = cubin;
+  s.funcs[{key, dev}] = fn;
+  return fn;
+}
+
+// ============================================================================
+// planning and launch
+// ============================================================================
+static void compute_magic(int64_t d, uint64_t& word) {
+  // s = ceil(log2 d); m = 2^32 (2^s - d) / d + 1 (valid for d, x < 2^31)
+  uint32_t sh = 0;
+  while ((1ull << sh) < (uint64_t)d) ++sh;
+  const uint64_t m = ((1ull << 32) * ((1ull << sh) - (uint64_t)d)) / (uint64_t)d + 1ull;
+  word = (uint64_t)(uint32_t)m | ((uint64_t)sh << 32);
+}
+
+static bool aligned(const void* p, int64_t a) { return a <= 1 || ((uintptr_t)p % (uintptr_t)a) == 0; }
+
+// chooses NCA_VEC and operand modes for a vector axis (the innermost canonical dim)
+static void plan_vec(const Space& s, Spec& sp, int max_vec_elems, bool with_out) {
+  const int ax = s.nd - 1;
+  int maxsz = 1;
+  if (with_out) maxsz = std::max(maxsz, dtinfo(s.out.dtype).size);
+  for (int k = 0; k < sp.nops; ++k)
+    if (s.ops[k].st[ax] == dtinfo(s.ops[k].dtype).size) maxsz = std::max(maxsz, dtinfo(s.ops[k].dtype).size);
+  int vec = std::max(1, std::min(max_vec_elems, 16 / maxsz));
+  auto out_ok = [&](int v) {
+    if (!with_out) return true;
+    const int64_t isz = dtinfo(s.out.dtype).size;
+    if (s.out.st[ax] != isz) return false;
+    if (!aligned(s.out.base, v * isz)) return false;
+    for (int d = 0; d < ax; ++d) if (s.out.st[d] % (v * isz) != 0) return false;
+    return true;
+  };
+  while (vec > 1 && (s.shape[ax] % vec != 0 || !out_ok(vec))) vec >>= 1;
+  sp.vec = vec;
+  sp.op_modes.assign(sp.nops, M_STRIDED);
+  for (int k = 0; k < sp.nops; ++k) {
+    const CArr& a = s.ops[k];
+    const int64_t isz = dtinfo(a.dtype).size;
+    if (a.st[ax] == 0) { sp.op_modes[k] = M_CONST; continue; }
+    if (vec == 1) { sp.op_modes[k] = M_STRIDED; continue; }
+    bool ok = a.st[ax] == isz && aligned(a.base, vec * isz);
+    for (int d = 0; d < ax && ok; ++d) if (a.st[d] % (vec * isz) != 0) ok = false;
+    sp.op_modes[k] = ok ? M_CONTIG : M_STRIDED;
+  }
+}
+
+static void fill_common_words(const Space& s, const Spec& sp, const Tape& t, const WordLayout& L,
+                              std::vector<uint64_t>& w) {
+  w.assign(L.nwords, 0);
+  for (int k = 0; k < sp.nops; ++k) {
+    w[L.opb + k] = (uint64_t)(uintptr_t)s.ops[k].base;
+    for (int d = 0; d < sp.nd; ++d) w[L.ops + k * sp.nd + d] = (uint64_t)s.ops[k].st[d];
+  }
+  if (s.has_out) {
+    w[L.outb] = (uint64_t)(uintptr_t)s.out.base;
+    for (int d = 0; d < sp.nd; ++d) w[L.outs + d] = (uint64_t)s.out.st[d];
+  }
+  for (int d = 0; d < sp.nd; ++d) w[L.shape + d] = (uint64_t)s.shape[d];
+  for (int i = 0; i < sp.nscal; ++i) w[L.scal + i] = scalar_word(sp.w, t.scalar_dtypes[i], t.scalar_slots[i]);
+  for (int k = 0; k < sp.nred; ++k) {
+    w[L.redb + k] = (uint64_t)(uintptr_t)s.reds[k].base;
+    for (int d = 0; d < sp.nd; ++d) w[L.reds + k * sp.nd + d] = (uint64_t)s.reds[k].st[d];
+  }
+  w[L.total] = (uint64_t)s.total();
+}
+
+static void launch(CUfunction fn, int64_t grid, std::vector<uint64_t>& words, cudaStream_t stream) {
+  if (grid <= 0) return;
+  count_launch();
+  if (grid > 0x7fffffffLL) fail(NCA_ERR_LIMIT, "grid too large");
+  void* params[] = {words.data()};
+  check_cu(drv().cuLaunchKernel(fn, (unsigned)grid, 1, 1, 256, 1, 1, 0, (CUstream)stream, params, nullptr),
+           "cuLaunchKernel");
+}
+
+static int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+static void check_broadcast(const int64_t* lshape, int n, const nca_view& v, const char* what) {
+  if (v.ndim > n) fail(NCA_ERR_SHAPE, "%s has %d dims, more than the result's %d", what, v.ndim, n);
+  for (int d = 0; d < v.ndim; ++d) {
+    const int ld = d + (n - v.ndim);
+    if (v.shape[d] != 1 && v.shape[d] != lshape[ld])
+      fail(NCA_ERR_SHAPE, "%s axis %d has extent %lld, result has %lld", what, d, (long long)v.shape[d], (long long)lshape[ld]);
+  }
+}
+
+static int broadcast_shape(const nca_view* ops, int nops, int64_t* out) {
+  int n = 0;
+  for (int k = 0; k < nops; ++k) n = std::max(n, (int)ops[k].ndim);
+  for (int d = 0; d < n; ++d) out[d] = 1;
+  for (int k = 0; k < nops; ++k) {
+    for (int d = 0; d < ops[k].ndim; ++d) {
+      const int ld = d + (n - ops[k].ndim);
+      const int64_t e = ops[k].shape[d];
+      if (e == 1) continue;
+      if (out[ld] == 1) out[ld] = e;
+      else if (out[ld] != e) fail(NCA_ERR_SHAPE, "operands do not broadcast on axis %d", ld);
+    }
+  }
+  return n;
+}
+
+void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& out, cudaStream_t stream) {
+  check_view(out, "out");
+  if (nops < 0 || nops > NCA_MAX_OPERANDS) fail(NCA_ERR_LIMIT, "%d operands (0..%d)", nops, NCA_MAX_OPERANDS);
+  if (tape.n_arrays > nops) fail(NCA_ERR_INVALID, "tape loads more operands than given");
+  for (int k = 0; k < nops; ++k) { check_view(ops[k], "operand"); check_broadcast(out.shape, out.ndim, ops[k], "operand"); }
+  int64_t n = 1;
+  for (int d = 0; d < out.ndim; ++d) n *= out.shape[d];
+  if (n == 0) return;
+  Space s = make_space(out.shape, out.ndim, ops, nops, &out, 0, nullptr, 0);
+  if (!tape.uses_idx && s.nd > 1) {
+    std::vector<int> perm(s.nd);
+    for (int d = 0; d < s.nd; ++d) perm[d] = d;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) {
+      return std::llabs(s.out.st[a]) > std::llabs(s.out.st[b]);
+    });
+    permute_dims(s, perm);
+  }
+  merge_dims(s);
+  ensure_nd1(s);
+  Spec sp;
+  sp.nops = nops; sp.nd = s.nd; sp.has_out = true; sp.out_dtype = out.dtype; sp.w = tape.compute_dtype;
+  sp.r = tape.result_dtype; sp.nscal = (int)tape.scalar_dtypes.size();
+  for (int k = 0; k < nops; ++k) sp.op_dtypes.push_back(ops[k].dtype);
+  bool flat = s.nd == 1 && s.out.st[0] == dtinfo(out.dtype).size;
+  for (int k = 0; k < nops && flat; ++k)
+    if (s.ops[k].st[0] != 0 && s.ops[k].st[0] != dtinfo(ops[k].dtype).size) flat = false;
+  plan_vec(s, sp, 16, true);
+  if (flat) {
+    for (int k = 0; k < nops; ++k) if (sp.op_modes[k] == M_STRIDED && sp.vec > 1) flat = false;
+  }
+  sp.kind = flat ? 1 : 2;
+  const int64_t total = s.total();
+  bool small_dims = true;
+  for (int d = 0; d < s.nd; ++d) if (s.shape[d] >= (1ll << 31)) small_dims = false;
+  sp.idx32 = (total / sp.vec < (1ll << 31) && small_dims) ? 1 : 0;
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, 0);
+  std::vector<uint64_t> w;
+  fill_common_words(s, sp, tape, L, w);
+  for (int d = 0; d < s.nd; ++d) {
+    int64_t dv = s.shape[d];
+    if (d == s.nd - 1) dv /= sp.vec;
+    compute_magic(dv, w[L.magic + d]);
+  }
+  CUfunction fn = jit_get(gen_source(sp, tape), "nca_kernel");
+  const int dev = current_device();
+  const int64_t groups = total / sp.vec;
+  int64_t grid = std::min<int64_t>(cdiv(std::max<int64_t>(groups, 1), 256), (int64_t)sm_count(dev) * 16);
+  launch(fn, grid, w, stream);
+}
+
+int reduce_out_dtype(int op, int in_dt) {
+  switch (op) {
+    case NCA_RED_SUM: return sum_dtype(in_dt);
+    case NCA_RED_MEAN: return NCA_FLOAT64;
+    case NCA_RED_MAX: case NCA_RED_MIN: return arith_dtype(in_dt);
+    case NCA_RED_ARGMAX: case NCA_RED_ARGMIN: return NCA_INT64;
+  }
+  fail(NCA_ERR_INVALID, "unknown reduction op %d", op);
+}
+
+void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
+                 const nca_reduction* reds, int nred, cudaStream_t stream) {
+  if (nred < 1 || nred > NCA_MAX_REDUCTIONS) fail(NCA_ERR_LIMIT, "%d reductions (1..%d)", nred, NCA_MAX_REDUCTIONS);
+  if (nops < 0 || nops > NCA_MAX_OPERANDS) fail(NCA_ERR_LIMIT, "%d operands (0..%d)", nops, NCA_MAX_OPERANDS);
+  if (tape.n_arrays > nops) fail(NCA_ERR_INVALID, "tape loads more operands than given");
+  for (int k = 0; k < nops; ++k) check_view(ops[k], "operand");
+  int64_t lshape[NCA_MAX_NDIM];
+  int n;
+  if (out) {
+    check_view(*out, "expr_out");
+    n = out->ndim;
+    for (int d = 0; d < n; ++d) lshape[d] = out->shape[d];
+  } else {
+    n = broadcast_shape(ops, nops, lshape);
+  }
+  for (int k = 0; k < nops; ++k) check_broadcast(lshape, n, ops[k], "operand");
+  const uint32_t all = n >= 32 ? 0xffffffffu : ((1u << n) - 1u);
+  const uint32_t mask = reds[0].axes_mask & all;
+  int kept_count = 0;
+  for (int d = 0; d < n; ++d) if (!((mask >> d) & 1u)) ++kept_count;
+  bool has_sum = false, has_max = false, has_min = false;
+  uint32_t red_ops = 0;
+  for (int k = 0; k < nred; ++k) {
+    if ((reds[k].axes_mask & all) != mask) fail(NCA_ERR_INVALID, "all reductions of one call must share axes_mask");
+    const int op = reds[k].op;
+    const int want = reduce_out_dtype(op, tape.result_dtype);
+    const nca_view& ov = reds[k].out;
+    check_view(ov, "reduction out");
+    if (ov.dtype != want)
+      fail(NCA_ERR_DTYPE, "reduction %d writes dtype %d, expected %s", k, ov.dtype, dtinfo(want).name);
+    if (ov.ndim != kept_count && !(kept_count == 0 && ov.ndim == 1 && ov.shape[0] == 1))
+      fail(NCA_ERR_SHAPE, "reduction %d output has %d dims, expected %d", k, ov.ndim, kept_count);
+    int kd = 0;
+    for (int d = 0; d < n && kept_count > 0; ++d) {
+      if ((mask >> d) & 1u) continue;
+      if (ov.shape[kd] != lshape[d]) fail(NCA_ERR_SHAPE, "reduction %d output extent mismatch on axis %d", k, d);
+      ++kd;
+    }
+    if (op == NCA_RED_SUM || op == NCA_RED_MEAN) has_sum = true;
+    if (op == NCA_RED_MAX || op == NCA_RED_ARGMAX) has_max = true;
+    if (op == NCA_RED_MIN || op == NCA_RED_ARGMIN) has_min = true;
+    red_ops |= (uint32_t)op << (4 * k);
+  }
+  // reduction views with kept_count==0 but ndim 1: treat their stride as unused
+  std::vector<nca_reduction> rv(reds, reds + nred);
+  for (auto& r : rv) if (kept_count == 0) { r.out.ndim = 0; }
+  int64_t KN = 1, RN = 1;
+  for (int d = 0; d < n; ++d) { if ((mask >> d) & 1u) RN *= lshape[d]; else KN *= lshape[d]; }
+  if (KN == 0) return;
+  Space s = make_space(lshape, n, ops, nops, out, mask, rv.data(), nred);
+  const int dev = current_device();
+  const int sms = sm_count(dev);
+  Spec sp;
+  sp.nops = nops; sp.has_out = out != nullptr; sp.out_dtype = out ? out->dtype : 0; sp.w = tape.compute_dtype;
+  sp.r = tape.result_dtype; sp.nscal = (int)tape.scalar_dtypes.size(); sp.nred = nred; sp.red_ops = red_ops;
+  sp.has_sum = has_sum; sp.has_max = has_max; sp.has_min = has_min;
+  for (int k = 0; k < nops; ++k) sp.op_dtypes.push_back(ops[k].dtype);
+  merge_dims(s);
+  ensure_nd1(s);
+  const bool inner_reduced = (RN == 0) || s.red[s.nd - 1];
+  if (inner_reduced && out) fail(NCA_ERR_UNSUPPORTED, "storing the expression while reducing its innermost axis is not supported; reduce without expr_out");
+  if (inner_reduced) {
+    // order [kept..., reduced...]
+    std::vector<int> perm;
+    for (int d = 0; d < s.nd; ++d) if (!s.red[d]) perm.push_back(d);
+    for (int d = 0; d < s.nd; ++d) if (s.red[d]) perm.push_back(d);
+    bool identity = true;
+    for (int d = 0; d < s.nd; ++d) if (perm[d] != d) identity = false;
+    if (!identity) {
+      if (tape.uses_idx) fail(NCA_ERR_UNSUPPORTED, "IDX in a reduction whose kept axes follow reduced axes");
+      permute_dims(s, perm);
+      merge_dims(s);
+    }
+    sp.nd = s.nd;
+    sp.kind = 3;
+    int nkept = 0;
+    for (int d = 0; d < s.nd; ++d) if (!s.red[d]) ++nkept;
+    sp.nkept = nkept;
+    for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
+    if (RN > 0) plan_vec(s, sp, 16, false); else { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
+    if (sp.vec > 1 && s.shape[s.nd - 1] % sp.vec != 0) { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
+    sp.team = RN >= 4096 ? 256 : 32;
+    const int64_t tpb = 256 / sp.team;
+    const int64_t target = (int64_t)sms * tpb * 4;
+    int64_t S = 1;
+    if (KN < target && RN > 0) {
+      S = cdiv(target, KN);
+      S = std::min<int64_t>(S, std::max<int64_t>(1, RN / ((int64_t)sp.team * sp.vec * 8)));
+    }
+    int64_t C = RN > 0 ? cdiv(RN, S) : 0;
+    C = cdiv(C, sp.vec) * sp.vec;
+    if (C > 0) S = cdiv(RN, C);
+    if (S < 1) S = 1;
+    const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+    std::vector<uint64_t> w;
+    fill_common_words(s, sp, tape, L, w);
+    w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+    StreamScratch part(S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0, stream);
+    if (S > 1) {
+      uint64_t* p = (uint64_t*)part.ptr;
+      if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
+      if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+      if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+    }
+    CUfunction fn = jit_get(gen_source(sp, tape), "nca_kernel");
+    launch(fn, cdiv(KN * S, tpb), w, stream);
+    if (S > 1) {
+      Spec fs = sp; fs.kind = 5;
+      CUfunction ff = jit_get(gen_source(fs, tape), "nca_kernel");
+      launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
+    }
+    return;
+  }
+  // innermost dim kept: RED_OUTER
+  sp.nd = s.nd;
+  sp.kind = 4;
+  for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
+  plan_vec(s, sp, 4, out != nullptr);
+  const int64_t KG = KN / sp.vec;
+  const int64_t target = (int64_t)sms * 1024;
+  int64_t S = 1;
+  if (KG < target) S = std::min<int64_t>(cdiv(target, KG), std::max<int64_t>(1, RN / 8));
+  int64_t C = cdiv(RN, S);
+  S = cdiv(RN, C);
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  std::vector<uint64_t> w;
+  fill_common_words(s, sp, tape, L, w);
+  w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+  StreamScratch part(S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0, stream);
+  if (S > 1) {
+    uint64_t* p = (uint64_t*)part.ptr;
+    if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
+    if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+    if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+  }
+  CUfunction fn = jit_get(gen_source(sp, tape), "nca_kernel");
+  launch(fn, cdiv(KG * S, 256), w, stream);
+  if (S > 1) {
+    Spec fs = sp; fs.kind = 5;
+    CUfunction ff = jit_get(gen_source(fs, tape), "nca_kernel");
+    launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
+  }
+}
+
+}  // namespace nca
+
+namespace nca {
+
+// Generates and NVRTC-compiles one kernel of every class for `arch` without a
+// device (the compile-only check of the template). Returns the number compiled.
+int jit_selftest(const char* arch) {
+  const std::string a = arch ? arch : "sm_103a";
+  int n = 0;
+  // tape: a*b + sqrt(abs(c)) - 0.5*a  (C1 shape of ops)
+  Tape t;
+  auto I = [](int op, int idx) { return (uint32_t)(op << 24) | (uint32_t)idx; };
+  t.instrs = {I(NCA_OP_LOAD_NCARR, 0), I(NCA_OP_LOAD_NCARR, 1), I(NCA_OP_MUL, 0),
+              I(NCA_OP_LOAD_NCARR, 2), I(NCA_OP_ABS, 0), I(NCA_OP_SQRT, 0), I(NCA_OP_ADD, 0),
+              I(NCA_OP_LOAD_CONST, 0), I(NCA_OP_LOAD_NCARR, 0), I(NCA_OP_MUL, 0), I(NCA_OP_SUB, 0)};
+  t.scalar_dtypes = {NCA_FLOAT64};
+  double half = 0.5; uint64_t hb; memcpy(&hb, &half, 8);
+  t.scalar_slots = {hb};
+  t.n_arrays = 3;
+  const int dts[][4] = {  // w, out/r, op dtype, vec
+      {NCA_FLOAT64, NCA_FLOAT64, NCA_FLOAT64, 2}, {NCA_FLOAT32, NCA_FLOAT32, NCA_INT32, 4},
+      {NCA_INT32, NCA_INT32, NCA_INT32, 4},       {NCA_FLOAT32, NCA_BFLOAT16, NCA_BFLOAT16, 4},
+      {NCA_UINT8, NCA_BOOL, NCA_UINT8, 16},       {NCA_INT64, NCA_INT64, NCA_INT16, 2}};
+  for (auto& d : dts) {
+    t.compute_dtype = d[0];
+    t.result_dtype = d[1];
+    for (int kind = 1; kind <= 5; ++kind) {
+      Spec sp;
+      sp.kind = kind; sp.nops = 3; sp.nd = kind == 1 ? 1 : 3; sp.vec = kind == 4 ? std::min(d[3], 4) : d[3];
+      sp.idx32 = 1; sp.w = d[0]; sp.r = d[1]; sp.out_dtype = d[1]; sp.nscal = 1;
+      sp.op_dtypes = {d[2], d[2], d[2]};
+      sp.op_modes = {M_CONTIG, M_CONST, M_STRIDED};
+      if (kind == 1) sp.op_modes = {M_CONTIG, M_CONST, M_CONTIG};
+      sp.has_out = kind <= 2 || kind == 4;
+      if (kind >= 3) {
+        sp.nred = 4; sp.red_ops = 0 | (2u << 4) | (4u << 8) | (1u << 12);
+        sp.has_sum = sp.has_max = true;
+        if (kind == 3) { sp.nkept = 1; sp.kept_mask = 1u; sp.red_ops = 3u | (5u << 4) | (0u << 8) | (1u << 12); sp.has_min = true; sp.has_max = false; }
+        else sp.kept_mask = 1u | 4u;
+      }
+      const std::string src = gen_source(sp, t);
+      nvrtc_compile(src, a);
+      ++n;
+    }
+  }
+  return n;
+}
+
+}  // namespace nca

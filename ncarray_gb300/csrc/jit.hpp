@@ -1,0 +1,51 @@
+// Expression/reduction engine of libncgb300: tape validation, canonical
+// iteration space, source generation, NVRTC compilation with an in-memory and
+// on-disk cubin cache, and kernel launch.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "common.hpp"
+
+namespace nca {
+
+// Tape after validation, with the reference's evaluation types resolved.
+struct Tape {
+  std::vector<uint32_t> instrs;
+  std::vector<int> scalar_dtypes;
+  std::vector<uint64_t> scalar_slots;
+  int compute_dtype = NCA_FLOAT64;
+  int result_dtype = NCA_FLOAT64;
+  bool uses_idx = false;
+  int n_arrays = 0;  // 1 + highest LOAD_NCARR/LOAD_SOARR index
+};
+
+Tape make_tape(const nca_tape* t, int n_operands);
+
+// out = tape(operands)
+void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& out,
+               cudaStream_t stream);
+
+// one pass: optional out, reductions sharing one axes mask
+void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
+                 const nca_reduction* reds, int nred, cudaStream_t stream);
+
+// expected output dtype of a reduction op over values of dtype `in_dt`
+int reduce_out_dtype(int op, int in_dt);
+
+// JIT statistics and cache directory
+void jit_stats(int64_t* compiled, int64_t* disk_hits, int64_t* mem_hits);
+void jit_set_cache_dir(const char* dir);
+std::string jit_cache_dir();
+
+// Compiles (or fetches) a kernel named `name` from CUDA source for the current
+// device. Used by the JIT engine and available to other modules.
+CUfunction jit_get(const std::string& source, const char* name);
+
+}  // namespace nca
+
+namespace nca {
+int jit_selftest(const char* arch);
+}
