@@ -332,13 +332,22 @@ class DevExpr:
         return e
 
     def _append(self, other: "DevExpr") -> None:
-        na, ns = len(self.arrays), len(self.scalars)
-        self.arrays += other.arrays
+        # an operand view that is already on the tape is loaded through the same
+        # index (one load per element instead of two)
+        keys = {_view_key(a): i for i, a in enumerate(self.arrays)}
+        remap = []
+        for a in other.arrays:
+            k = _view_key(a)
+            if k not in keys:
+                keys[k] = len(self.arrays)
+                self.arrays.append(a)
+            remap.append(keys[k])
+        ns = len(self.scalars)
         self.scalars += other.scalars
         for ins in other.instrs:
             op, idx = ins >> 24, ins & 0xFFFFFF
             if op in (OpCode.LOAD_NCARR, OpCode.LOAD_SOARR):
-                ins = (op << 24) | (idx + na)
+                ins = (op << 24) | remap[idx]
             elif op == OpCode.LOAD_CONST:
                 ins = (op << 24) | (idx + ns)
             self.instrs.append(ins)
@@ -484,6 +493,10 @@ class DevExpr:
 
     def argmin(self, axes=None):
         return self._reduce(RedOp.ARGMIN, axes)
+
+
+def _view_key(a: NCDevArray):
+    return (a.ptr, int(a.dtype), a.shape, a.strides)
 
 
 def _axes_mask(axes, ndim: int):

@@ -397,7 +397,7 @@ static std::string gen_eval(const Tape& t) {
     switch (op) {
       case NCA_OP_NOOP: break;
       case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR: st.push_back("v[" + std::to_string(idx) + "][q]"); break;
-      case NCA_OP_LOAD_CONST: st.push_back("s[" + std::to_string(idx) + "]"); break;
+      case NCA_OP_LOAD_CONST: st.push_back("nca_word<nca_w>(s[" + std::to_string(idx) + "])"); break;
       case NCA_OP_IDX: push_tmp("(nca_w)lin"); break;
       default: {
         const int ar = op_arity(op);
@@ -515,7 +515,7 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << g.str() << "}\n";
   os << "__device__ __forceinline__ void nca_gather1(const NcaArgs& A, const i64* off, nca_w (*v)[NCA_VEC]) {\n"
      << g1.str() << "}\n";
-  os << "__device__ __forceinline__ nca_w nca_eval(const nca_w (*v)[NCA_VEC], int q, const nca_w* s, i64 lin) {\n"
+  os << "__device__ __forceinline__ nca_w nca_eval(const nca_w (*v)[NCA_VEC], int q, const u64* s, i64 lin) {\n"
      << "  (void)v; (void)q; (void)s; (void)lin;\n"
      << gen_eval(t) << "}\n";
 

@@ -289,6 +289,11 @@ int orc_expr_eval(const uint32_t* instrs, int n_instrs, const int* scalar_dtypes
   for (int k = 0; k < nops; ++k) dts[k] = ops[k].dtype;
   char* ob = vbase(out);
   if (!bitwise_ok(instrs, n_instrs)) return 4;
+  for (int i = 0; i < n_instrs; ++i) {
+    const int op = (int)(instrs[i] >> 24), ix = (int)(instrs[i] & 0xffffff);
+    if ((op == OP_LOAD_NCARR || op == OP_LOAD_SOARR) && ix >= nops) return 5;
+    if (op == OP_LOAD_CONST && ix >= n_scalars) return 5;
+  }
   switch (compute_dtype) {
     case D_BOOL: RUN_EVAL(b8)
     case D_CHAR: case D_I8: RUN_EVAL(i8)

@@ -59,6 +59,7 @@ def assert_bits_equal(got: np.ndarray, want: np.ndarray, what: str = "") -> None
 
 def oracle_eval(orc, expr, host_ops):
     """Evaluates a DevExpr's tape on the host operands with the oracle."""
+    assert len(host_ops) == len(expr.arrays), "one host operand per tape operand"
     return orc.expr_eval(expr.instrs, expr.scalars, int(compute_dtype(expr.expr_dtype, expr.work)),
                          [(h, int(a.dtype)) for h, a in zip(host_ops, expr.arrays)], expr.shape,
                          int(expr.expr_dtype))
