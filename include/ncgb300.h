@@ -164,6 +164,17 @@ int32_t nca_expr_reduce(const nca_tape* tape, const nca_view* operands, int32_t 
 int32_t nca_reduce(const nca_view* src, int32_t op, uint32_t axes_mask,
                    const nca_view* out, void* stream);
 
+/* Full reduction of a C-contiguous float32/float64/int32/int64 view that
+ * allocates no device memory: for callers that cannot call cudaMalloc or
+ * cudaMallocAsync (stream capture that forbids memory nodes, pre-planned
+ * real-time loops, hosts that give the library no allocator). No counterpart
+ * in the reference. Its per-CTA partials live in a fixed 64 KiB device array
+ * inside the library; inputs above 2^31 elements return NCA_ERR_LIMIT. The
+ * first call on a device takes that array's address (make it before any
+ * stream capture). Calls share the array: calls that overlap on the GPU race.
+ * `out` is one element of the dtype nca_reduce would write. */
+int32_t nca_reduce_noalloc(const nca_view* src, int32_t op, const nca_view* out, void* stream);
+
 /* dst = cast(src) view to view: GPUEngine::execute_assign / execute_copy_into
  * (gpuengine.hh:377-637; kernels.cuh:613-644). */
 int32_t nca_copy(const nca_view* src, const nca_view* dst, void* stream);

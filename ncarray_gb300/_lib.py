@@ -69,12 +69,14 @@ EXPORTS = {
     "nca_last_error": (c_char_p, []),
     "nca_version": (c_int32, []),
     "nca_launch_count": (c_int64, []),
+    "nca_device_status": (c_int32, [POINTER(c_int32), c_void_p]),
     "nca_jit_stats": (c_int32, [POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
     "nca_jit_set_cache_dir": (c_int32, [c_char_p]),
     "nca_jit_selftest": (c_int32, [c_char_p, POINTER(c_int32)]),
     "nca_expr_eval": (c_int32, [POINTER(Tape), POINTER(View), c_int32, POINTER(View), c_void_p]),
     "nca_expr_reduce": (c_int32, [POINTER(Tape), POINTER(View), c_int32, POINTER(View), POINTER(Reduction), c_int32, c_void_p]),
     "nca_reduce": (c_int32, [POINTER(View), c_int32, c_uint32, POINTER(View), c_void_p]),
+    "nca_reduce_noalloc": (c_int32, [POINTER(View), c_int32, POINTER(View), c_void_p]),
     "nca_copy": (c_int32, [POINTER(View), POINTER(View), c_void_p]),
     "nca_fill": (c_int32, [POINTER(View), c_int32, c_void_p, c_void_p]),
     "nca_stencil3d": (c_int32, [POINTER(View), POINTER(View), POINTER(c_double), c_double, c_void_p]),
