@@ -129,6 +129,11 @@ const char* nca_last_error(void);
 int32_t nca_version(void);
 /* Number of kernels launched by this library in this process (all entry points). */
 int64_t nca_launch_count(void);
+/* Reads and clears the status word that bounded device waits set when they
+ * give up (0 = none gave up, NCA_ERR_TIMEOUT otherwise); synchronises `stream`.
+ * The reference has no device-side failure reporting (it exits or throws on
+ * launch errors only: rtcompiler.hh:68-88, gpuengine.hh:156-158). */
+int32_t nca_device_status(int32_t* status, void* stream);
 /* Number of JIT kernels compiled / loaded from the disk cache / found in memory. */
 int32_t nca_jit_stats(int64_t* compiled, int64_t* disk_hits, int64_t* mem_hits);
 /* Directory of the on-disk cubin cache (NULL resets to the default). Replaces

@@ -8,6 +8,10 @@
 
 using namespace nca;
 
+namespace nca {
+int stencil_read_status(cudaStream_t s);
+}
+
 extern "C" {
 
 const char* nca_last_error(void) { return last_error().c_str(); }
@@ -15,6 +19,13 @@ const char* nca_last_error(void) { return last_error().c_str(); }
 int32_t nca_version(void) { return 1000; }
 
 int64_t nca_launch_count(void) { return launch_count(); }
+
+int32_t nca_device_status(int32_t* status, void* stream) {
+  return guarded([&] {
+    if (!status) fail(NCA_ERR_INVALID, "null status");
+    *status = stencil_read_status((cudaStream_t)stream);
+  });
+}
 
 int32_t nca_jit_stats(int64_t* compiled, int64_t* disk_hits, int64_t* mem_hits) {
   return guarded([&] { jit_stats(compiled, disk_hits, mem_hits); });

@@ -1,0 +1,494 @@
+// Batched reductions over many arrays of uneven length (float32 / bfloat16 /
+// float16): per array sum, mean, max and sum(x*x - x).
+//
+// ncarray has no batched API (a list of arrays must share one shape:
+// src/lib/pyncarray/utilities.hh:271-314); issued through its GPUEngine, each
+// reduction of each array is one synchronous launch (gpuengine.hh:301-333).
+// Here the whole batch is one persistent launch:
+//   - nca_batch_create splits every array into chunks of `chunk_bytes` and
+//     uploads a descriptor table (array, first element, element count) once;
+//   - the persistent kernel's CTAs walk the chunk table with a static stride
+//     (chunks carry equal bytes, so the walk is balanced); each CTA reduces its
+//     chunk with per-thread float-float sums (Knuth TwoSum) of x and of
+//     fma(x, x, -x), a float max, and a float64 block tree, then writes one
+//     partial record;
+//   - the CTA finishing the last chunk of an array (a per-array counter
+//     incremented after a release fence) combines that array's partials in
+//     chunk order (deterministic) and resets the counter for the next launch.
+// There is no waiting anywhere, so nothing can hang. The schedule (chunk
+// bytes, threads, unroll, CTAs per SM) comes from an autotuner whose choices are
+// cached per shape class in a text file next to the JIT cache.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "common.hpp"
+#include "jit.hpp"
+
+struct nca_batch {
+  int n = 0;
+  int dev = 0;
+  std::vector<nca_batch_item> items;
+  // device tables
+  void* d_items = nullptr;    // ItemDev[n]
+  void* d_chunks = nullptr;   // ChunkDev[nchunks]
+  void* d_parts = nullptr;    // PartDev[nchunks]
+  void* d_done = nullptr;     // unsigned[n]
+  long long nchunks = 0;
+  // schedule
+  long long chunk_bytes = 256 * 1024;
+  int threads = 256, unroll = 4, ctas_per_sm = 4;
+  std::string shape_class;
+  // graph
+  cudaGraphExec_t graph = nullptr;
+  cudaStream_t capture_stream = nullptr;
+  void* graph_results = nullptr;
+};
+
+namespace {
+
+struct ItemDev {
+  const void* data;
+  long long length;
+  int dtype;
+  int first_chunk;
+  int nchunks;
+  int pad;
+};
+
+struct ChunkDev {
+  int item;
+  int index;        // chunk number within the item
+  long long begin;  // first element
+  long long count;  // elements
+};
+
+struct PartDev {
+  double s, q;   // sum(x), sum(x*x - x)
+  float mx;      // max (lowest() if none above it)
+  int pad;
+};
+
+__device__ __forceinline__ float ld_elem(const void* p, long long i, int dt) {
+  if (dt == NCA_FLOAT32) return __ldcs(static_cast<const float*>(p) + i);
+  const unsigned short h = __ldcs(static_cast<const unsigned short*>(p) + i);
+  if (dt == NCA_BFLOAT16) return __uint_as_float(((unsigned)h) << 16);
+  float f;
+  asm("{.reg .b16 t; mov.b16 t, %1; cvt.f32.f16 %0, t;}" : "=f"(f) : "h"(h));
+  return f;
+}
+
+struct FF {  // float-float accumulator
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
+    hi = s;
+  }
+  __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
+};
+
+__device__ __forceinline__ float lowest_f() { return __uint_as_float(0xff7fffffu); }
+
+// Reduces chunk c of its item into a PartDev (valid in thread 0).
+template <int UNROLL>
+__device__ PartDev reduce_chunk(const ItemDev& it, const ChunkDev& c) {
+  FF s, q;
+  float mx = lowest_f();
+  const int T = blockDim.x;
+  const long long end = c.begin + c.count;
+  long long i = c.begin + threadIdx.x;
+  // unrolled main loop: UNROLL independent loads in flight per thread
+  for (; i + (long long)(UNROLL - 1) * T < end; i += (long long)UNROLL * T) {
+    float v[UNROLL];
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) v[u] = ld_elem(it.data, i + (long long)u * T, it.dtype);
+#pragma unroll
+    for (int u = 0; u < UNROLL; ++u) {
+      s.add(v[u]);
+      q.add(__fmaf_rn(v[u], v[u], -v[u]));
+      mx = v[u] > mx ? v[u] : mx;
+    }
+  }
+  for (; i < end; i += T) {
+    const float v = ld_elem(it.data, i, it.dtype);
+    s.add(v);
+    q.add(__fmaf_rn(v, v, -v));
+    mx = v > mx ? v : mx;
+  }
+  double ds = s.get(), dq = q.get();
+  for (int off = 16; off > 0; off >>= 1) {
+    ds += __shfl_down_sync(0xffffffffu, ds, off);
+    dq += __shfl_down_sync(0xffffffffu, dq, off);
+    const float om = __shfl_down_sync(0xffffffffu, mx, off);
+    mx = om > mx ? om : mx;
+  }
+  __shared__ double sh_s[32], sh_q[32];
+  __shared__ float sh_m[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (T + 31) >> 5;
+  __syncthreads();
+  if (lane == 0) { sh_s[wid] = ds; sh_q[wid] = dq; sh_m[wid] = mx; }
+  __syncthreads();
+  PartDev p{0.0, 0.0, lowest_f(), 0};
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < nw; ++k) {   // fixed order: deterministic
+      p.s += sh_s[k];
+      p.q += sh_q[k];
+      p.mx = sh_m[k] > p.mx ? sh_m[k] : p.mx;
+    }
+  }
+  return p;
+}
+
+template <int UNROLL>
+__global__ void batch_persistent_kernel(const ItemDev* __restrict__ items, const ChunkDev* __restrict__ chunks,
+                                        long long nchunks, PartDev* __restrict__ parts, unsigned* __restrict__ done,
+                                        nca_batch_result* __restrict__ results) {
+  __shared__ int s_last;
+  for (long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const ChunkDev ch = chunks[c];
+    const ItemDev it = items[ch.item];
+    const PartDev p = reduce_chunk<UNROLL>(it, ch);
+    if (threadIdx.x == 0) {
+      parts[c] = p;
+      __threadfence();
+      const unsigned prev = atomicAdd(done + ch.item, 1u);
+      s_last = (prev + 1 == (unsigned)it.nchunks) ? 1 : 0;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+      __threadfence();
+      double s = 0.0, q = 0.0;
+      float mx = lowest_f();
+      for (int k = 0; k < it.nchunks; ++k) {   // chunk order; L2 reads (written by other SMs)
+        const PartDev* pk = parts + it.first_chunk + k;
+        s += __ldcg(&pk->s);
+        q += __ldcg(&pk->q);
+        const float m = __ldcg(&pk->mx);
+        mx = m > mx ? m : mx;
+      }
+      nca_batch_result r;
+      r.sum = s;
+      r.mean = s / (double)it.length;
+      r.max = (double)mx;
+      r.sum_sq_m = q;
+      results[ch.item] = r;
+      done[ch.item] = 0u;   // ready for the next launch
+    }
+    __syncthreads();
+  }
+}
+
+// ---- plain form: one launch per op per array, float64 accumulation ----------------
+// OP 0: sum, 1: max, 2: sum(x*x - x); mean is sum / length (a fourth launch).
+template <int OP>
+__global__ void plain_kernel(const void* data, long long n, int dt, double* out) {
+  double acc = OP == 1 ? -1.0e300 : 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = (double)ld_elem(data, i, dt);
+    if (OP == 0) acc += v;
+    if (OP == 1) acc = v > acc ? v : acc;
+    if (OP == 2) acc += v * v - v;
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    const double o = __shfl_down_sync(0xffffffffu, acc, off);
+    if (OP == 1) acc = o > acc ? o : acc; else acc += o;
+  }
+  __shared__ double sh[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = OP == 1 ? -1.0e300 : 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) r = OP == 1 ? (sh[k] > r ? sh[k] : r) : r + sh[k];
+    if (OP == 1) {
+      // ordered max on the bit pattern of a double
+      unsigned long long b = (unsigned long long)__double_as_longlong(r);
+      b = (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+      atomicMax(reinterpret_cast<unsigned long long*>(out), b);
+    } else {
+      atomicAdd(out, r);
+    }
+  }
+}
+
+__global__ void plain_init_kernel(nca_batch_result* r, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { r[i].sum = 0.0; r[i].mean = 0.0; r[i].max = 0.0; r[i].sum_sq_m = 0.0; }
+}
+
+__global__ void plain_mean_kernel(nca_batch_result* r, const ItemDev* items, int i) {
+  r[i].mean = r[i].sum / (double)items[i].length;
+  unsigned long long b = (unsigned long long)__double_as_longlong(r[i].max);
+  // the max slot holds the ordered bit pattern; 0 means no element
+  if (b == 0ull) { r[i].max = (double)lowest_f(); return; }
+  b = (b >> 63) ? (b & 0x7fffffffffffffffull) : ~b;
+  r[i].max = __longlong_as_double((long long)b);
+}
+
+void launch_persistent(nca_batch* B, nca_batch_result* results, cudaStream_t s) {
+  const int grid = (int)std::min<long long>(B->nchunks, (long long)nca::sm_count(B->dev) * B->ctas_per_sm);
+  if (grid <= 0) return;
+  const ItemDev* it = (const ItemDev*)B->d_items;
+  const ChunkDev* ch = (const ChunkDev*)B->d_chunks;
+  PartDev* pa = (PartDev*)B->d_parts;
+  unsigned* dn = (unsigned*)B->d_done;
+  switch (B->unroll) {
+    case 1: batch_persistent_kernel<1><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
+    case 2: batch_persistent_kernel<2><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
+    case 8: batch_persistent_kernel<8><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
+    default: batch_persistent_kernel<4><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
+  }
+  nca::check_cuda(cudaGetLastError(), "batched kernel launch");
+  nca::count_launch();
+}
+
+void free_tables(nca_batch* B) {
+  if (B->d_chunks) cudaFree(B->d_chunks);
+  if (B->d_parts) cudaFree(B->d_parts);
+  B->d_chunks = B->d_parts = nullptr;
+  if (B->graph) { cudaGraphExecDestroy(B->graph); B->graph = nullptr; }
+}
+
+// (re)builds the chunk table for the current chunk_bytes
+void build_chunks(nca_batch* B, cudaStream_t s) {
+  free_tables(B);
+  std::vector<ItemDev> items(B->n);
+  std::vector<ChunkDev> chunks;
+  for (int i = 0; i < B->n; ++i) {
+    const nca_batch_item& src = B->items[i];
+    const int isz = src.dtype == NCA_FLOAT32 ? 4 : 2;
+    const long long per = std::max<long long>(B->chunk_bytes / isz, 256);
+    items[i].data = src.data;
+    items[i].length = src.length;
+    items[i].dtype = src.dtype;
+    items[i].first_chunk = (int)chunks.size();
+    long long k = 0;
+    for (long long b = 0; b < src.length || (b == 0 && src.length == 0); b += per, ++k) {
+      ChunkDev c{i, (int)k, b, std::min(per, src.length - b)};
+      chunks.push_back(c);
+      if (src.length == 0) break;
+    }
+    items[i].nchunks = (int)k + (src.length == 0 ? 1 : 0);
+    items[i].pad = 0;
+  }
+  B->nchunks = (long long)chunks.size();
+  using nca::check_cuda;
+  if (!B->d_items) check_cuda(cudaMalloc(&B->d_items, sizeof(ItemDev) * std::max(B->n, 1)), "batch items");
+  if (!B->d_done) {
+    check_cuda(cudaMalloc(&B->d_done, sizeof(unsigned) * std::max(B->n, 1)), "batch counters");
+    check_cuda(cudaMemsetAsync(B->d_done, 0, sizeof(unsigned) * std::max(B->n, 1), s), "batch counters");
+  }
+  check_cuda(cudaMalloc(&B->d_chunks, sizeof(ChunkDev) * std::max<long long>(B->nchunks, 1)), "batch chunks");
+  check_cuda(cudaMalloc(&B->d_parts, sizeof(PartDev) * std::max<long long>(B->nchunks, 1)), "batch partials");
+  check_cuda(cudaMemcpyAsync(B->d_items, items.data(), sizeof(ItemDev) * B->n, cudaMemcpyHostToDevice, s), "items");
+  check_cuda(cudaMemcpyAsync(B->d_chunks, chunks.data(), sizeof(ChunkDev) * B->nchunks, cudaMemcpyHostToDevice, s),
+             "chunks");
+  check_cuda(cudaStreamSynchronize(s), "batch tables");
+}
+
+std::string shape_class(const nca_batch* B) {
+  long long bytes = 0, n16 = 0;
+  for (auto& it : B->items) {
+    bytes += it.length * (it.dtype == NCA_FLOAT32 ? 4 : 2);
+    if (it.dtype != NCA_FLOAT32) ++n16;
+  }
+  const int lb = bytes > 0 ? (int)std::log2((double)bytes) : 0;
+  const int ln = B->n > 0 ? (int)std::log2((double)B->n) : 0;
+  const int mix = B->n > 0 ? (int)(4.0 * n16 / B->n + 0.5) : 0;
+  std::ostringstream os;
+  os << "batch_b" << lb << "_n" << ln << "_m" << mix;
+  return os.str();
+}
+
+std::string tune_file() { return nca::jit_cache_dir() + "/batch_tune.txt"; }
+
+bool load_tuned(nca_batch* B) {
+  std::ifstream f(tune_file());
+  std::string key;
+  long long cb;
+  int th, un, cps;
+  bool found = false;
+  while (f >> key >> cb >> th >> un >> cps) {
+    if (key == B->shape_class) {
+      B->chunk_bytes = cb; B->threads = th; B->unroll = un; B->ctas_per_sm = cps;
+      found = true;
+    }
+  }
+  return found;
+}
+
+void store_tuned(const nca_batch* B) {
+  std::ofstream f(tune_file(), std::ios::app);
+  if (f) f << B->shape_class << " " << B->chunk_bytes << " " << B->threads << " " << B->unroll << " "
+           << B->ctas_per_sm << "\n";
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t nca_batch_create(const nca_batch_item* items, int32_t n_items, nca_batch** out, void* stream) {
+  return nca::guarded([&] {
+    using namespace nca;
+    if (!out) fail(NCA_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (n_items < 0 || (n_items > 0 && !items)) fail(NCA_ERR_INVALID, "bad item list");
+    if (n_items > (1 << 30)) fail(NCA_ERR_LIMIT, "too many items");
+    for (int i = 0; i < n_items; ++i) {
+      const auto& it = items[i];
+      if (it.dtype != NCA_FLOAT32 && it.dtype != NCA_BFLOAT16 && it.dtype != NCA_FLOAT16)
+        fail(NCA_ERR_DTYPE, "item %d: batched reductions take float32, bfloat16 or float16", i);
+      if (it.length < 0) fail(NCA_ERR_INVALID, "item %d: negative length", i);
+      if (it.length > 0 && !it.data) fail(NCA_ERR_INVALID, "item %d: null data", i);
+    }
+    auto* B = new nca_batch();
+    try {
+      B->n = n_items;
+      B->dev = current_device();
+      B->items.assign(items, items + n_items);
+      B->shape_class = shape_class(B);
+      load_tuned(B);
+      build_chunks(B, (cudaStream_t)stream);
+    } catch (...) {
+      nca_batch_destroy(B);
+      throw;
+    }
+    *out = B;
+  });
+}
+
+int32_t nca_batch_reduce(nca_batch* B, nca_batch_result* results, void* stream) {
+  return nca::guarded([&] {
+    if (!B || !results) nca::fail(NCA_ERR_INVALID, "null argument");
+    launch_persistent(B, results, (cudaStream_t)stream);
+  });
+}
+
+int32_t nca_batch_reduce_graph(nca_batch* B, nca_batch_result* results, void* stream) {
+  return nca::guarded([&] {
+    using namespace nca;
+    if (!B || !results) fail(NCA_ERR_INVALID, "null argument");
+    if (!B->graph || B->graph_results != results) {
+      if (B->graph) { cudaGraphExecDestroy(B->graph); B->graph = nullptr; }
+      if (!B->capture_stream) check_cuda(cudaStreamCreateWithFlags(&B->capture_stream, cudaStreamNonBlocking), "stream");
+      check_cuda(cudaStreamBeginCapture(B->capture_stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+      try {
+        launch_persistent(B, results, B->capture_stream);
+      } catch (...) {
+        cudaGraph_t g;
+        cudaStreamEndCapture(B->capture_stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      cudaGraph_t g = nullptr;
+      check_cuda(cudaStreamEndCapture(B->capture_stream, &g), "end capture");
+      cudaError_t e = cudaGraphInstantiate(&B->graph, g, 0);
+      cudaGraphDestroy(g);
+      check_cuda(e, "graph instantiate");
+      B->graph_results = results;
+    }
+    check_cuda(cudaGraphLaunch(B->graph, (cudaStream_t)stream), "graph launch");
+    count_launch();
+  });
+}
+
+int32_t nca_batch_reduce_plain(nca_batch* B, nca_batch_result* results, void* stream) {
+  return nca::guarded([&] {
+    using namespace nca;
+    if (!B || !results) fail(NCA_ERR_INVALID, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (B->n == 0) return;
+    plain_init_kernel<<<(B->n + 255) / 256, 256, 0, s>>>(results, B->n);
+    count_launch();
+    const int sms = sm_count(B->dev);
+    for (int i = 0; i < B->n; ++i) {
+      const auto& it = B->items[i];
+      const int grid = (int)std::max<long long>(1, std::min<long long>((it.length + 2047) / 2048, 2ll * sms));
+      double* r = &results[i].sum;
+      plain_kernel<0><<<grid, 256, 0, s>>>(it.data, it.length, it.dtype, r);
+      plain_kernel<1><<<grid, 256, 0, s>>>(it.data, it.length, it.dtype, &results[i].max);
+      plain_kernel<2><<<grid, 256, 0, s>>>(it.data, it.length, it.dtype, &results[i].sum_sq_m);
+      plain_mean_kernel<<<1, 1, 0, s>>>(results, (const ItemDev*)B->d_items, i);
+      count_launch(4);
+    }
+    check_cuda(cudaGetLastError(), "plain launches");
+  });
+}
+
+int32_t nca_batch_autotune(nca_batch* B, nca_batch_result* results, void* stream) {
+  return nca::guarded([&] {
+    using namespace nca;
+    if (!B || !results) fail(NCA_ERR_INVALID, "null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    struct Cand { long long cb; int th, un, cps; };
+    std::vector<Cand> cands;
+    for (long long cb : {128ll << 10, 256ll << 10, 512ll << 10, 1024ll << 10})
+      for (int th : {256, 512})
+        for (int un : {4, 8})
+          for (int cps : {2, 4})
+            if (th * cps <= 2048) cands.push_back({cb, th, un, cps});
+    cudaEvent_t e0, e1;
+    check_cuda(cudaEventCreate(&e0), "event");
+    check_cuda(cudaEventCreate(&e1), "event");
+    float best = 1e30f;
+    Cand bestc = cands[0];
+    for (const auto& c : cands) {
+      B->chunk_bytes = c.cb; B->threads = c.th; B->unroll = c.un; B->ctas_per_sm = c.cps;
+      build_chunks(B, s);
+      launch_persistent(B, results, s);   // warm-up
+      check_cuda(cudaEventRecord(e0, s), "record");
+      for (int r = 0; r < 3; ++r) launch_persistent(B, results, s);
+      check_cuda(cudaEventRecord(e1, s), "record");
+      check_cuda(cudaEventSynchronize(e1), "sync");
+      float ms = 0.f;
+      check_cuda(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+      if (ms < best) { best = ms; bestc = c; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    B->chunk_bytes = bestc.cb; B->threads = bestc.th; B->unroll = bestc.un; B->ctas_per_sm = bestc.cps;
+    build_chunks(B, s);
+    store_tuned(B);
+  });
+}
+
+int32_t nca_batch_schedule(const nca_batch* B, int64_t* chunk, int32_t* threads, int32_t* items_per_thread,
+                           int32_t* ctas) {
+  return nca::guarded([&] {
+    if (!B) nca::fail(NCA_ERR_INVALID, "null batch");
+    if (chunk) *chunk = B->chunk_bytes;
+    if (threads) *threads = B->threads;
+    if (items_per_thread) *items_per_thread = B->unroll;
+    if (ctas) *ctas = (int32_t)std::min<long long>(B->nchunks, (long long)nca::sm_count(B->dev) * B->ctas_per_sm);
+  });
+}
+
+int32_t nca_batch_status(nca_batch* B, int32_t* status, void* stream) {
+  return nca::guarded([&] {
+    if (!B || !status) nca::fail(NCA_ERR_INVALID, "null argument");
+    // the persistent kernel never waits on another CTA, so it has no timeout
+    // path: the status is that of the stream
+    nca::check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "batch stream");
+    *status = 0;
+  });
+}
+
+void nca_batch_destroy(nca_batch* B) {
+  if (!B) return;
+  free_tables(B);
+  if (B->d_items) cudaFree(B->d_items);
+  if (B->d_done) cudaFree(B->d_done);
+  if (B->capture_stream) cudaStreamDestroy(B->capture_stream);
+  delete B;
+}
+
+}  // extern "C"

@@ -1,0 +1,98 @@
+"""2-D histogram and batched uneven reductions on the GPU vs the oracle.
+
+Histogram counts (uint64) must be bit-exact; per-bin weight sums are float64
+accumulations rounded to float32, so they match the float64 oracle to one
+float32 rounding (|got - ref| <= 2^-24 |ref|, plus one ulp of slack).
+Batched results are float64: |err| <= 1e-6 |ref| for the mean and both sums
+(and <= 1e-9 sum|x| in absolute terms); max is exact."""
+import numpy as np
+import pytest
+
+import ncarray_gb300 as nca
+from ncarray_gb300.batch import Batch
+from ncarray_gb300.hist import hist2d
+from tests.helpers import SEED
+
+pytestmark = pytest.mark.gpu
+
+
+def mixture_points(rng, n):
+    centres = rng.uniform(0, 1, (8, 2))
+    sigma = rng.uniform(0.01, 0.1, 8)
+    weights = rng.dirichlet(np.full(8, 0.5))
+    comp = rng.choice(8, size=n, p=weights)
+    pts = centres[comp] + rng.normal(size=(n, 2)) * sigma[comp, None]
+    return pts[:, 0].astype(np.float32), pts[:, 1].astype(np.float32)
+
+
+@pytest.mark.parametrize("n,nb", [(1 << 20, (1024, 1024)), (100003, (37, 61)), (5, (4, 4))])
+def test_hist2d_matches_oracle(cuda, orc, n, nb):
+    rng = np.random.default_rng(SEED + 5)
+    x, y = mixture_points(rng, n)
+    x[: min(n, 3)] = [np.nan, -0.5, 1.0][: min(n, 3)]
+    w = rng.lognormal(0, 1, n).astype(np.float32)
+    nbx, nby = nb
+    counts, wsum = hist2d(nca.NCDevArray.from_host(x), nca.NCDevArray.from_host(y), nbx, nby,
+                          w=nca.NCDevArray.from_host(w))
+    rc, rw = orc.hist2d(x, y, w, nbx, nby, 0.0, 1.0, 0.0, 1.0)
+    assert np.array_equal(counts.to_host().reshape(-1), rc)
+    got = wsum.to_host().reshape(-1).astype(np.float64)
+    ref32 = rw.astype(np.float32).astype(np.float64)
+    assert np.all(np.abs(got - ref32) <= 2.0**-23 * np.abs(rw) + 1e-30)
+    # counts only (no weights)
+    c2, _ = hist2d(nca.NCDevArray.from_host(x), nca.NCDevArray.from_host(y), nbx, nby)
+    assert np.array_equal(c2.to_host().reshape(-1), rc)
+
+
+def make_batch(rng, n, lo=64, hi=1 << 16):
+    lens = np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), n))).astype(np.int64)
+    lens[:3] = [1, 64, 257][: min(n, 3)]
+    arrays, host, dts = [], [], []
+    for i, L in enumerate(lens):
+        x = (np.exp(rng.normal(0, 2, L)) * rng.choice([-1.0, 1.0], L)).astype(np.float32)
+        if i % 2 == 0:
+            arrays.append(nca.NCDevArray.from_host(x))
+            host.append(x)
+            dts.append(10)
+        else:
+            b = (x.view(np.uint32) >> 16).astype(np.uint16)
+            arrays.append(nca.NCDevArray.from_host(b, nca.DType.bfloat16))
+            host.append(b)
+            dts.append(22)
+    return arrays, host, dts
+
+
+def check_batch(got, ref, host, dts):
+    for i in range(len(host)):
+        x = host[i]
+        xf = (x.astype(np.uint32) << 16).view(np.float32) if dts[i] == 22 else x
+        scale = float(np.abs(xf.astype(np.float64)).sum())
+        for k in (0, 1, 3):
+            assert abs(got[i, k] - ref[i, k]) <= 1e-6 * abs(ref[i, k]) + 1e-9 * scale, (i, k, got[i], ref[i])
+        assert got[i, 2] == ref[i, 2]
+
+
+def test_batch_persistent_graph_plain(cuda, orc):
+    rng = np.random.default_rng(SEED + 6)
+    arrays, host, dts = make_batch(rng, 300)
+    ref = orc.batch_reduce(host, dts, nthreads=4)
+    b = Batch(arrays)
+    check_batch(b.run().to_host(), ref, host, dts)
+    check_batch(b.run().to_host(), ref, host, dts)              # counters reset between launches
+    check_batch(b.run(graph=True).to_host(), ref, host, dts)
+    check_batch(b.run(graph=True).to_host(), ref, host, dts)
+    check_batch(b.run_plain().to_host(), ref, host, dts)
+    sched = b.autotune()
+    assert sched["chunk_bytes"] > 0 and sched["threads"] in (256, 512)
+    check_batch(b.run().to_host(), ref, host, dts)
+
+
+def test_batch_relative_error_with_cancellation(cuda, orc):
+    """Random-sign lognormal(0, 2) sums: the float-float path stays within 1e-6
+    of float64 relative to |sum| on every array of the batch."""
+    rng = np.random.default_rng(SEED + 7)
+    arrays, host, dts = make_batch(rng, 64, lo=1 << 12, hi=1 << 20)
+    ref = orc.batch_reduce(host, dts, nthreads=4)
+    got = Batch(arrays).run().to_host()
+    rel = np.abs(got[:, 0] - ref[:, 0]) / np.abs(ref[:, 0])
+    assert rel.max() <= 1e-6, rel.max()
