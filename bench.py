@@ -9,7 +9,9 @@ Headline workload (strided/broadcast fusion, float32 + int32):
 Inputs are resident in HBM when the timed region starts; the working set
 (~640 MB) is larger than L2, so no flush is needed between steps.
 
-`value` = algorithmic bytes of a step / device time of a step (GB/s, whole job).
+`value` = algorithmic bytes of a step / device time of a step (GB/s, whole job);
+          the step's C-ABI calls are captured once into a CUDA graph and the
+          timed region replays it K times.
 `e2e`   = the same bytes through the C-ABI calls with pinned HOST buffers:
           each step copies x, v, k in and y, max, argmax, z out.
 `--impl reference` times the CPU restatement of the reference path (the
@@ -127,10 +129,12 @@ class C2Step:
         self.y = nca.NCDevArray(self.y_expr.shape, self.y_expr.dtype)
         self.z = nca.NCDevArray(self.z_expr.shape, self.z_expr.dtype)
         self.red = [(nca.RedOp.MAX, 2), (nca.RedOp.ARGMAX, 2)]
-        self.mx = self.am = None
+        kept = (self.y.shape[0], self.y.shape[1], self.y.shape[3])
+        self.mx = nca.NCDevArray(kept, nca.DType.float32)
+        self.am = nca.NCDevArray(kept, nca.DType.int64)
 
     def fused(self):
-        self.mx, self.am = self.y_expr.evaluate(out=self.y, reductions=self.red)
+        self.y_expr.evaluate(out=self.y, reductions=self.red, red_out=[self.mx, self.am])
 
     def intexpr(self):
         self.z_expr.evaluate(out=self.z)
@@ -138,6 +142,23 @@ class C2Step:
     def __call__(self):
         self.fused()
         self.intexpr()
+
+
+def make_graph(torch, fn):
+    """Captures fn() (a sequence of C-ABI calls on the current stream) into a
+    CUDA graph; the kernels are compiled beforehand by eager calls."""
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        fn()
+        fn()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    torch.cuda.synchronize()
+    return g
 
 
 def time_events(torch, fn, reps: int) -> float:
@@ -175,6 +196,273 @@ def cpu_baseline_c2(nthreads: int | None = None, sample_l0: int = 1):
     dt = time.perf_counter() - t0
     gbs = c2_bytes(n)["step"] / dt / 1e9
     return gbs, n, dt
+
+
+# ---- per-op measurements of the other workloads -----------------------------------
+def flush_l2(torch, buf):
+    buf.fill_(1)   # 512 MiB write > L2
+
+
+def timed_flushed(torch, fn, reps, flush_buf):
+    """Average device ms of fn() with an L2 flush before every rep (flush not timed)."""
+    s = torch.cuda.current_stream()
+    total = 0.0
+    for _ in range(reps):
+        flush_l2(torch, flush_buf)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        fn()
+        b.record(s)
+        torch.cuda.synchronize()
+        total += a.elapsed_time(b)
+    return total / reps
+
+
+def op_entry(bytes_, ms, peak, **extra):
+    gbs = bytes_ / (ms * 1e-3) / 1e9
+    d = {"GB/s": round(gbs, 1), "frac_of_measured": round(gbs / peak, 4), "ms": round(ms, 4)}
+    d.update(extra)
+    return d
+
+
+def measure_c1(torch, nca, peak, flush_buf, reps=20):
+    """C1: out = a*b + sqrt(abs(c)) - 0.5*a on float64 (128,128,128), with the
+    axis-0 sum and max in the same pass, then the full sum and max."""
+    rng = np.random.default_rng(SEED + 0)
+    a, b, c = (rng.uniform(-1, 1, (128, 128, 128)) for _ in range(3))
+    da, db, dc = (nca.NCDevArray.from_host(v) for v in (a, b, c))
+    with nca.lazy_mode():
+        e = da * db + nca.sqrt(abs(dc)) - 0.5 * da
+    out = nca.NCDevArray(e.shape, e.dtype)
+    res = {}
+
+    def step():
+        s0, m0 = e.evaluate(out=out, reductions=[(nca.RedOp.SUM, 0), (nca.RedOp.MAX, 0)])
+        res["s"] = s0._expr().evaluate(reductions=[(nca.RedOp.SUM, None)])[0]
+        res["m"] = m0._expr().evaluate(reductions=[(nca.RedOp.MAX, None)])[0]
+
+    for _ in range(3):
+        step()
+    ms = timed_flushed(torch, step, reps, flush_buf)
+    n = a.size
+    ref = a * b + np.sqrt(np.abs(c)) - np.float32(0.5) * a
+    exact = bool(np.array_equal(out.to_host(), ref))
+    rel = abs(float(res["s"].to_host()) - float(np.sum(ref))) / abs(float(np.sum(ref)))
+    return op_entry(32 * n + 2 * 8 * 128 * 128, ms, peak, bound_note="float64 ALU (GB300 FP64 rate) rather than HBM",
+                    out_bit_exact=exact, sum_rel_err_vs_f64=rel, max_exact=bool(float(res["m"].to_host()) == ref.max()),
+                    l2="flushed before every rep")
+
+
+def measure_c3(torch, nca, peak, iters=10):
+    """C3: 7- and 27-point Laplacian, 512^3 float32, zero halo, 10 Jacobi steps
+    u <- u + 0.1 L(u); error vs the float64 run of the same steps."""
+    from ncarray_gb300.stencil import Stencil3D, laplacian7, laplacian27, device_status
+    g = torch.Generator(device="cuda").manual_seed(SEED + 2)
+    n = 512 ** 3
+    u64 = torch.randn((512, 512, 512), generator=g, device="cuda", dtype=torch.float64)
+    out = {}
+    for name, w in (("7pt", laplacian7()), ("27pt", laplacian27())):
+        st = Stencil3D(w, 0.1)
+        a = nca.NCDevArray((512, 512, 512), nca.DType.float32)
+        b = nca.NCDevArray((512, 512, 512), nca.DType.float32)
+        src32 = u64.float().contiguous()
+        a._buf.view(torch.float32).view(512, 512, 512).copy_(src32)
+        st.iterate(a, b, 2)
+        a._buf.view(torch.float32).view(512, 512, 512).copy_(src32)
+        s = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        res = st.iterate(a, b, iters)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / iters
+        status = device_status()
+        # float64 run of the same steps on the device
+        a64 = nca.NCDevArray((512, 512, 512), nca.DType.float64)
+        b64 = nca.NCDevArray((512, 512, 512), nca.DType.float64)
+        a64._buf.view(torch.float64).view(512, 512, 512).copy_(src32.double())
+        r64 = st.iterate(a64, b64, iters)
+        t32 = res._buf.view(torch.float32).double()
+        t64 = r64._buf.view(torch.float64)
+        rel_l2 = float(torch.linalg.vector_norm(t32 - t64) / torch.linalg.vector_norm(t64))
+        max_rel = float((t32 - t64).abs().max() / t64.abs().max())
+        out[name] = op_entry(8 * n, ms, peak, per="iteration", rel_l2_err_vs_f64=rel_l2, max_err_rel_to_max=max_rel,
+                             status=status)
+        del a, b, a64, b64, t32, t64
+    return out
+
+
+def c4_points(torch, nca):
+    """2^27 (x, y) float32 points from a mixture of 8 Gaussians (centres
+    uniform in [0,1)^2, sigma 0.01-0.1, Dirichlet(0.5) weights) and lognormal
+    weights, generated on the device from a seed."""
+    P = 1 << 27
+    rng = np.random.default_rng(SEED + 3)
+    centres = rng.uniform(0, 1, (8, 2))
+    sigma = rng.uniform(0.01, 0.1, 8)
+    mix = rng.dirichlet(np.full(8, 0.5))
+    g = torch.Generator(device="cuda").manual_seed(SEED + 3)
+    comp = torch.multinomial(torch.tensor(mix, device="cuda", dtype=torch.float32), P, replacement=True, generator=g)
+    cen = torch.tensor(centres, device="cuda", dtype=torch.float32)[comp]
+    sig = torch.tensor(sigma, device="cuda", dtype=torch.float32)[comp]
+    pts = cen + torch.randn((P, 2), generator=g, device="cuda") * sig[:, None]
+    wts = torch.exp(torch.randn(P, generator=g, device="cuda"))
+    x = nca.NCDevArray((P,), nca.DType.float32)
+    y = nca.NCDevArray((P,), nca.DType.float32)
+    w = nca.NCDevArray((P,), nca.DType.float32)
+    x._buf.view(torch.float32).copy_(pts[:, 0].contiguous())
+    y._buf.view(torch.float32).copy_(pts[:, 1].contiguous())
+    w._buf.view(torch.float32).copy_(wts)
+    del comp, cen, sig, pts, wts
+    return x, y, w
+
+
+def measure_c4(torch, nca, peak, reps=5):
+    """C4: 2^27 (x, y) float32 points from 8 Gaussians into 1024 x 1024 bins on
+    [0,1)^2; uint64 counts (exact) and float32 weighted sums (float32
+    compensated per tile, float64 across tiles)."""
+    from ncarray_gb300.hist import hist2d_into
+    P = 1 << 27
+    x, y, w = c4_points(torch, nca)
+    counts = nca.NCDevArray((1024, 1024), nca.DType.uint64)
+    wsum = nca.NCDevArray((1024, 1024), nca.DType.float32)
+
+    def run(weighted):
+        counts.fill(0)
+        if weighted:
+            wsum.fill(0.0)
+        hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0), w if weighted else None, wsum if weighted else None)
+
+    out = {}
+    for weighted in (False, True):
+        run(weighted)
+        s = torch.cuda.current_stream()
+        tot = 0.0
+        for _ in range(reps):
+            counts.fill(0)
+            if weighted:
+                wsum.fill(0.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0), w if weighted else None, wsum if weighted else None)
+            e1.record(s)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        ms = tot / reps
+        byts = (12 * P + 16 * 1024 * 1024) if weighted else (8 * P + 8 * 1024 * 1024)
+        out["weighted" if weighted else "counts"] = op_entry(byts, ms, peak, points=P)
+    total = int(counts._buf.view(torch.int64).sum().item())
+    out["counts_total"] = total
+    return out
+
+
+def measure_c5(torch, nca, peak, n_arrays=20000):
+    """C5: 20,000 1-D arrays, lengths log-uniform in [64, 2^22], half float32 and
+    half bfloat16, x = s * exp(N(0, 2)) with random signs; per array sum, mean,
+    max and sum(x*x - x): one persistent graph-replayed launch vs the plain
+    per-array per-op float64 launches."""
+    import oracle
+    from ncarray_gb300.batch import Batch
+    rng = np.random.default_rng(SEED + 4)
+    lens = np.round(np.exp(rng.uniform(np.log(64), np.log(2 ** 22), n_arrays))).astype(np.int64)
+    is16 = np.arange(n_arrays) % 2 == 1
+    g = torch.Generator(device="cuda").manual_seed(SEED + 4)
+    tot32, tot16 = int(lens[~is16].sum()), int(lens[is16].sum())
+    buf32 = torch.empty(tot32, device="cuda", dtype=torch.float32)
+    buf16 = torch.empty(tot16, device="cuda", dtype=torch.bfloat16)
+    for buf, tot in ((buf32, tot32), (buf16, tot16)):
+        step = 1 << 28
+        for o in range(0, tot, step):
+            m = min(step, tot - o)
+            v = torch.exp(torch.randn(m, generator=g, device="cuda") * 2.0)
+            v *= torch.where(torch.rand(m, generator=g, device="cuda") < 0.5, -1.0, 1.0)
+            buf[o:o + m].copy_(v)
+            del v
+    arrays, o32, o16 = [], 0, 0
+    b32 = buf32.view(torch.uint8)
+    b16 = buf16.view(torch.uint8)
+    for i, L in enumerate(lens):
+        L = int(L)
+        if is16[i]:
+            arrays.append(nca.NCDevArray((L,), nca.DType.bfloat16, _buf=b16, _offset=2 * o16))
+            o16 += L
+        else:
+            arrays.append(nca.NCDevArray((L,), nca.DType.float32, _buf=b32, _offset=4 * o32))
+            o32 += L
+    nbytes = 4 * tot32 + 2 * tot16
+    B = Batch(arrays)
+    sched = B.autotune()
+    B.run(graph=True)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+
+    def timeit(fn, reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ms_b = timeit(lambda: B.run(graph=True), 5)
+    got = B.run(graph=True).to_host().copy()
+    ms_p = timeit(B.run_plain, 1)
+    plain = B.results.to_host().copy()
+    # accuracy vs float64 on a sample of arrays (copied to the host)
+    pick = rng.choice(n_arrays, size=min(400, n_arrays), replace=False)
+    host, dts = [], []
+    for i in pick:
+        a = arrays[i]
+        raw = a._buf[a._offset: a._offset + a.nbytes].cpu().numpy()
+        host.append(raw.view(np.float32) if a.dtype == nca.DType.float32 else raw.view(np.uint16))
+        dts.append(10 if a.dtype == nca.DType.float32 else 22)
+    ref = oracle.batch_reduce(host, dts, nthreads=omp_threads())
+    g_ = got[pick]
+    p_ = plain[pick]
+    rel = lambda a_, b_: float(np.max(np.abs(a_ - b_) / np.maximum(np.abs(b_), 1e-300)))  # noqa: E731
+    return op_entry(nbytes, ms_b, peak, arrays=n_arrays, bytes=nbytes, plain_ms=round(ms_p, 3),
+                    speedup_vs_plain=round(ms_p / ms_b, 2), schedule=sched,
+                    batched_max_rel_err={"sum": rel(g_[:, 0], ref[:, 0]), "mean": rel(g_[:, 1], ref[:, 1]),
+                                         "sum_x2_minus_x": rel(g_[:, 3], ref[:, 3]),
+                                         "max_exact": bool(np.array_equal(g_[:, 2], ref[:, 2]))},
+                    plain_max_rel_err={"sum": rel(p_[:, 0], ref[:, 0]), "sum_x2_minus_x": rel(p_[:, 3], ref[:, 3])},
+                    sample_checked=len(pick))
+
+
+def profile_op(torch, nca, op: str, steps: int) -> None:
+    """Runs one op `steps` times at the bench size, with no timing or JSON:
+    the target of small, self-terminating profiler captures."""
+    if op in ("c2-fused", "c2-int"):
+        x, v, k = c2_host()
+        step = C2Step(nca, nca.NCDevArray.from_host(x), nca.NCDevArray.from_host(v), nca.NCDevArray.from_host(k))
+        fn = step.fused if op == "c2-fused" else step.intexpr
+    elif op in ("c3-7", "c3-27"):
+        from ncarray_gb300.stencil import Stencil3D, laplacian7, laplacian27
+        st = Stencil3D(laplacian7() if op == "c3-7" else laplacian27(), 0.1)
+        a = nca.NCDevArray((512, 512, 512), nca.DType.float32)
+        b = nca.NCDevArray((512, 512, 512), nca.DType.float32)
+        a._buf.view(torch.float32).normal_()
+        fn = lambda: st.apply(a, b)  # noqa: E731
+    elif op == "c1":
+        rng = np.random.default_rng(SEED)
+        da, db, dc = (nca.NCDevArray.from_host(rng.uniform(-1, 1, (128, 128, 128))) for _ in range(3))
+        with nca.lazy_mode():
+            e = da * db + nca.sqrt(abs(dc)) - 0.5 * da
+        out = nca.NCDevArray(e.shape, e.dtype)
+        fn = lambda: e.evaluate(out=out, reductions=[(nca.RedOp.SUM, 0), (nca.RedOp.MAX, 0)])  # noqa: E731
+    elif op == "c4":
+        from ncarray_gb300.hist import hist2d_into
+        x, y, w = c4_points(torch, nca)
+        counts = nca.NCDevArray((1024, 1024), nca.DType.uint64).fill(0)
+        wsum = nca.NCDevArray((1024, 1024), nca.DType.float32).fill(0.0)
+        fn = lambda: hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0), w, wsum)  # noqa: E731
+    else:
+        raise SystemExit(f"unknown --profile-op {op}")
+    for _ in range(steps):
+        fn()
+    torch.cuda.synchronize()
+    print(f"profile-op {op}: {steps} runs ok")
 
 
 def omp_threads() -> int:
@@ -219,6 +507,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--headline-only", action="store_true", help="skip the per-op measurements of the other workloads")
+    ap.add_argument("--profile-op", default=None, help="run one op --steps times for a profiler capture")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -240,6 +530,9 @@ def main():
     nbuild.build()
     import ncarray_gb300 as nca
     from ncarray_gb300 import _lib
+    if args.profile_op:
+        profile_op(torch, nca, args.profile_op, args.steps)
+        return
 
     x, v, k = c2_host()
     n = int(np.prod(k.shape))
@@ -259,11 +552,21 @@ def main():
     if not np.array_equal(step.am.to_host()[0], np.argmax(ref0, axis=1)):
         raise SystemExit("bench: argmax differs from the host formula")
 
+    # one step = one replay of the captured graph of the step's C-ABI calls
+    l0 = _lib.lib().nca_launch_count()
+    step()
+    torch.cuda.synchronize()
+    per_step_launches = _lib.lib().nca_launch_count() - l0
+    g_step = make_graph(torch, step)
+    g_fused = make_graph(torch, step.fused)
+    g_int = make_graph(torch, step.intexpr)
+    for _ in range(args.warmup):
+        g_step.replay()
+    torch.cuda.synchronize()
     dev_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[0] or 0) if world == 1 else local
     sampler = ClockSampler(dev_index)
     sampler.start()
     time.sleep(0.15)
-    launches0 = _lib.lib().nca_launch_count()
     s = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if dist:
@@ -271,16 +574,16 @@ def main():
     torch.cuda.synchronize()
     e0.record(s)
     for _ in range(args.steps):
-        step()
+        g_step.replay()
     e1.record(s)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     ms_total = e0.elapsed_time(e1)
-    launches = _lib.lib().nca_launch_count() - launches0
+    launches = per_step_launches * args.steps
     # per-kernel timing (dominant kernel = the fused pass) for the roofline
-    ms_fused = time_events(torch, step.fused, args.steps)
-    ms_int = time_events(torch, step.intexpr, args.steps)
+    ms_fused = time_events(torch, g_fused.replay, args.steps)
+    ms_int = time_events(torch, g_int.replay, args.steps)
     clocks = sampler.stop()
     if dist:
         t = torch.tensor([ms_total], device="cuda")
@@ -332,6 +635,22 @@ def main():
         cpu = {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"view slice 0 of 8 along axis 0 ({ns} elements), one step, {dt:.2f} s"}
 
+    per_op = {"c2_fused_expr_max_argmax": {"GB/s": round(fused_gbs, 1), "frac_of_measured": round(fused_gbs / peak, 4)},
+              "c2_int_expr": {"GB/s": round(int_gbs, 1), "frac_of_measured": round(int_gbs / peak, 4)}}
+    if not args.headline_only:
+        del step, dx, dv, dk
+        torch.cuda.empty_cache()
+        flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+        for name, fn in (("c1_fused_f64", lambda: measure_c1(torch, nca, peak, flush_buf)),
+                         ("c3_stencil_f32", lambda: measure_c3(torch, nca, peak)),
+                         ("c4_hist2d", lambda: measure_c4(torch, nca, peak)),
+                         ("c5_batched", lambda: measure_c5(torch, nca, peak))):
+            try:
+                per_op[name] = fn()
+            except Exception as ex:  # a failed side measurement must not hide the headline
+                per_op[name] = {"error": f"{type(ex).__name__}: {ex}"[:300]}
+            torch.cuda.empty_cache()
+
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
@@ -345,13 +664,13 @@ def main():
         "config": {"workload": "strided/broadcast fusion: x f32 (64,256,256,8) viewed (3,1,2,0) * v[None,:,None,None]"
                                " + k i32 (8,256,256,64); y stored + max/argmax axis 2 in one pass; (k*3+7)%11",
                    "elements": n, "bytes_per_step": by["step"], "l2": "working set 640 MB > L2; no flush",
+                   "launch": "each step is one replay of a CUDA graph of its C-ABI calls",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(fused_gbs, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(fused_gbs / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
                      "kernel": "fused expression + axis-2 max/argmax (JIT RED_OUTER)",
                      "bytes_per_launch": by["fused"], "ms_per_launch": round(ms_fused, 5)},
-        "per_op": {"c2_fused_expr_max_argmax": {"GB/s": round(fused_gbs, 1), "frac_of_measured": round(fused_gbs / peak, 4)},
-                   "c2_int_expr": {"GB/s": round(int_gbs, 1), "frac_of_measured": round(int_gbs / peak, 4)}},
+        "per_op": per_op,
         "gpu_launches": int(launches),
         "clocks": clocks,
         "e2e": e2e,

@@ -427,13 +427,23 @@ class DevExpr:
         self.evaluate(out=out)
         return out
 
-    def evaluate(self, out: Optional[NCDevArray] = None, reductions: Iterable = ()):
+    def _abi(self):
+        # the tape and operand descriptors never change once an expression is
+        # built (operators return new objects), so they are packed once
+        c = getattr(self, "_abi_cache", None)
+        if c is None:
+            t, keep = self._tape()
+            ops, n = self._operands()
+            c = self._abi_cache = (t, keep, ops, n)
+        return c
+
+    def evaluate(self, out: Optional[NCDevArray] = None, reductions: Iterable = (), red_out=None):
         """One fused pass: stores the value into `out` (if given) and computes
         the reductions, a sequence of (RedOp, axes or None). Returns the list of
-        reduction results (NCDevArray; 0-d for full reductions)."""
+        reduction results (NCDevArray; 0-d for full reductions), written into
+        `red_out` (arrays of the right shape and dtype) when it is given."""
         reductions = list(reductions)
-        t, keep = self._tape()
-        ops, n = self._operands()
+        t, _keep, ops, n = self._abi()
         stream = current_stream()
         if not reductions:
             if out is None:
@@ -443,11 +453,16 @@ class DevExpr:
             return []
         shape = out.shape if out is not None else self.shape
         results, rs = [], []
-        for op, axes in reductions:
+        for i, (op, axes) in enumerate(reductions):
             op = RedOp(op)
             mask, kept = _axes_mask(axes, len(shape))
             odt = _red_out_dtype(op, self.expr_dtype)
-            res = NCDevArray([shape[d] for d in kept], odt)
+            if red_out is not None:
+                res = red_out[i]
+                if res.dtype != odt or res.shape != tuple(shape[d] for d in kept):
+                    raise ValueError(f"reduction output {i} must be {odt.name} {[shape[d] for d in kept]}")
+            else:
+                res = NCDevArray([shape[d] for d in kept], odt)
             results.append(res)
             r = _lib.Reduction()
             r.op = int(op)

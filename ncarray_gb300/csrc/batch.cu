@@ -85,51 +85,124 @@ __device__ __forceinline__ float ld_elem(const void* p, long long i, int dt) {
   return f;
 }
 
-struct FF {  // float-float accumulator
-  float hi = 0.f, lo = 0.f;
-  __device__ __forceinline__ void add(float x) {
-    const float s = __fadd_rn(hi, x);
-    const float bb = __fsub_rn(s, hi);
-    lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
-    hi = s;
-  }
-  __device__ __forceinline__ double get() const { return (double)hi + (double)lo; }
-};
-
 __device__ __forceinline__ float lowest_f() { return __uint_as_float(0xff7fffffu); }
 
-// Reduces chunk c of its item into a PartDev (valid in thread 0).
-template <int UNROLL>
-__device__ PartDev reduce_chunk(const ItemDev& it, const ChunkDev& c) {
-  FF s, q;
-  float mx = lowest_f();
+// Two float-float accumulators held as float2 pairs (even / odd elements), so
+// every step of Knuth's TwoSum is one packed f32x2 instruction; a - b is
+// ffma2(b, -1, a), exact up to its single rounding.
+struct FF2 {
+  float2 hi = make_float2(0.f, 0.f), lo = make_float2(0.f, 0.f);
+  __device__ __forceinline__ void add(float2 x) {
+    const float2 m1 = make_float2(-1.f, -1.f);
+    const float2 s = __fadd2_rn(hi, x);
+    const float2 bb = __ffma2_rn(hi, m1, s);
+    const float2 e1 = __ffma2_rn(__ffma2_rn(bb, m1, s), m1, hi);
+    const float2 e2 = __ffma2_rn(bb, m1, x);
+    lo = __fadd2_rn(lo, __fadd2_rn(e1, e2));
+    hi = s;
+  }
+  __device__ __forceinline__ double get() const {
+    return ((double)hi.x + (double)lo.x) + ((double)hi.y + (double)lo.y);
+  }
+};
+
+struct Acc2 {
+  FF2 s, q;
+  float mx = -3.40282347e+38f;   // lowest float (bit pattern 0xff7fffff)
+  // a pair of elements (a missing one is passed as 0 with `two` false)
+  __device__ __forceinline__ void see(float2 x, bool two = true) {
+    s.add(x);
+    const float2 nx = make_float2(-x.x, -x.y);
+    q.add(__ffma2_rn(x, x, nx));
+    mx = fmaxf(mx, x.x);
+    if (two) mx = fmaxf(mx, x.y);
+  }
+};
+
+// 16 bytes -> float2 pairs: float32 gives 2 pairs, 16-bit types 4
+template <int DT> struct Vec;
+template <> struct Vec<NCA_FLOAT32> {
+  static constexpr int kElems = 4;
+  static __device__ __forceinline__ void unpack(const uint4& u, float2* o) {
+    o[0] = make_float2(__uint_as_float(u.x), __uint_as_float(u.y));
+    o[1] = make_float2(__uint_as_float(u.z), __uint_as_float(u.w));
+  }
+  static __device__ __forceinline__ float one(const void* p, long long i) { return __ldcs(static_cast<const float*>(p) + i); }
+};
+template <> struct Vec<NCA_BFLOAT16> {
+  static constexpr int kElems = 8;
+  static __device__ __forceinline__ float2 w2(unsigned w) {
+    return make_float2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+  }
+  static __device__ __forceinline__ void unpack(const uint4& u, float2* o) {
+    o[0] = w2(u.x); o[1] = w2(u.y); o[2] = w2(u.z); o[3] = w2(u.w);
+  }
+  static __device__ __forceinline__ float one(const void* p, long long i) {
+    return __uint_as_float(((unsigned)__ldcs(static_cast<const unsigned short*>(p) + i)) << 16);
+  }
+};
+template <> struct Vec<NCA_FLOAT16> {
+  static constexpr int kElems = 8;
+  static __device__ __forceinline__ float2 w2(unsigned w) {
+    float a, b;
+    asm("{.reg .b16 l, h; mov.b32 {l, h}, %2; cvt.f32.f16 %0, l; cvt.f32.f16 %1, h;}" : "=f"(a), "=f"(b) : "r"(w));
+    return make_float2(a, b);
+  }
+  static __device__ __forceinline__ void unpack(const uint4& u, float2* o) {
+    o[0] = w2(u.x); o[1] = w2(u.y); o[2] = w2(u.z); o[3] = w2(u.w);
+  }
+  static __device__ __forceinline__ float one(const void* p, long long i) {
+    const unsigned short h = __ldcs(static_cast<const unsigned short*>(p) + i);
+    float f;
+    asm("{.reg .b16 t; mov.b16 t, %1; cvt.f32.f16 %0, t;}" : "=f"(f) : "h"(h));
+    return f;
+  }
+};
+
+// Reduces chunk c of its item into a PartDev (valid in thread 0): a scalar head
+// up to the first 16-byte boundary, UNROLL 16-byte loads in flight per thread
+// over the aligned body, then a scalar tail.
+template <int DT, int UNROLL>
+__device__ PartDev reduce_chunk_t(const ItemDev& it, const ChunkDev& c) {
+  using V = Vec<DT>;
+  constexpr int isz = DT == NCA_FLOAT32 ? 4 : 2;
+  Acc2 acc;
   const int T = blockDim.x;
-  const long long end = c.begin + c.count;
-  long long i = c.begin + threadIdx.x;
-  // unrolled main loop: UNROLL independent loads in flight per thread
-  for (; i + (long long)(UNROLL - 1) * T < end; i += (long long)UNROLL * T) {
-    float v[UNROLL];
+  const char* base = static_cast<const char*>(it.data);
+  const long long b = c.begin, e = c.begin + c.count;
+  const uintptr_t a0 = (uintptr_t)(base + b * isz);
+  long long head = (long long)(((16 - (a0 & 15)) & 15) / isz);
+  if (head > c.count) head = c.count;
+  const long long nv = (c.count - head) / V::kElems;          // aligned 16-byte vectors
+  const long long vb = b + head, ve = vb + nv * V::kElems;
+  if (threadIdx.x < head) acc.see(make_float2(V::one(it.data, b + threadIdx.x), 0.f), false);
+  const uint4* vp = reinterpret_cast<const uint4*>(base + vb * isz);
+  long long i = threadIdx.x;
+  for (; i + (long long)(UNROLL - 1) * T < nv; i += (long long)UNROLL * T) {
+    uint4 u[UNROLL];
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) v[u] = ld_elem(it.data, i + (long long)u * T, it.dtype);
+    for (int k = 0; k < UNROLL; ++k) u[k] = __ldcs(vp + i + (long long)k * T);
 #pragma unroll
-    for (int u = 0; u < UNROLL; ++u) {
-      s.add(v[u]);
-      q.add(__fmaf_rn(v[u], v[u], -v[u]));
-      mx = v[u] > mx ? v[u] : mx;
+    for (int k = 0; k < UNROLL; ++k) {
+      float2 f[V::kElems / 2];
+      V::unpack(u[k], f);
+#pragma unroll
+      for (int j = 0; j < V::kElems / 2; ++j) acc.see(f[j]);
     }
   }
-  for (; i < end; i += T) {
-    const float v = ld_elem(it.data, i, it.dtype);
-    s.add(v);
-    q.add(__fmaf_rn(v, v, -v));
-    mx = v > mx ? v : mx;
+  for (; i < nv; i += T) {
+    float2 f[V::kElems / 2];
+    V::unpack(__ldcs(vp + i), f);
+#pragma unroll
+    for (int j = 0; j < V::kElems / 2; ++j) acc.see(f[j]);
   }
-  double ds = s.get(), dq = q.get();
+  for (long long t = ve + threadIdx.x; t < e; t += T) acc.see(make_float2(V::one(it.data, t), 0.f), false);
+  double ds = acc.s.get(), dq = acc.q.get();
+  float mx = acc.mx;
   for (int off = 16; off > 0; off >>= 1) {
     ds += __shfl_down_sync(0xffffffffu, ds, off);
     dq += __shfl_down_sync(0xffffffffu, dq, off);
-    const float om = __shfl_down_sync(0xffffffffu, mx, off);
-    mx = om > mx ? om : mx;
+    mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
   }
   __shared__ double sh_s[32], sh_q[32];
   __shared__ float sh_m[32];
@@ -142,10 +215,17 @@ __device__ PartDev reduce_chunk(const ItemDev& it, const ChunkDev& c) {
     for (int k = 0; k < nw; ++k) {   // fixed order: deterministic
       p.s += sh_s[k];
       p.q += sh_q[k];
-      p.mx = sh_m[k] > p.mx ? sh_m[k] : p.mx;
+      p.mx = fmaxf(p.mx, sh_m[k]);
     }
   }
   return p;
+}
+
+template <int UNROLL>
+__device__ PartDev reduce_chunk(const ItemDev& it, const ChunkDev& c) {
+  if (it.dtype == NCA_FLOAT32) return reduce_chunk_t<NCA_FLOAT32, UNROLL>(it, c);
+  if (it.dtype == NCA_BFLOAT16) return reduce_chunk_t<NCA_BFLOAT16, UNROLL>(it, c);
+  return reduce_chunk_t<NCA_FLOAT16, UNROLL>(it, c);
 }
 
 template <int UNROLL>

@@ -100,6 +100,7 @@ const Driver& drv() {
     resolve("cuModuleGetFunction", r.cuModuleGetFunction);
     resolve("cuLaunchKernel", r.cuLaunchKernel);
     resolve("cuFuncSetAttribute", r.cuFuncSetAttribute);
+    resolve("cuOccupancyMaxActiveBlocksPerMultiprocessor", r.cuOccupancyMaxActiveBlocksPerMultiprocessor);
     resolve("cuGetErrorString", r.cuGetErrorString);
     resolve("cuTensorMapEncodeTiled", r.cuTensorMapEncodeTiled);
     return r;

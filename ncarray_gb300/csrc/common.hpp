@@ -76,6 +76,7 @@ struct Driver {
   CUresult (*cuLaunchKernel)(CUfunction, unsigned, unsigned, unsigned, unsigned, unsigned,
                              unsigned, unsigned, CUstream, void**, void**);
   CUresult (*cuFuncSetAttribute)(CUfunction, CUfunction_attribute, int);
+  CUresult (*cuOccupancyMaxActiveBlocksPerMultiprocessor)(int*, CUfunction, int, size_t);
   CUresult (*cuGetErrorString)(CUresult, const char**);
   CUresult (*cuTensorMapEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                      const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,

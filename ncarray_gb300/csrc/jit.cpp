@@ -276,7 +276,7 @@ static void ensure_nd1(Space& s) {
 // ============================================================================
 // source generation
 // ============================================================================
-enum { M_CONTIG = 0, M_CONST = 1, M_STRIDED = 2 };
+enum { M_CONTIG = 0, M_CONST = 1, M_STRIDED = 2, M_STAGED = 3 };
 
 struct Spec {
   int kind = 1, nops = 0, nd = 1, vec = 1, idx32 = 0, nkept = 0, team = 256;
@@ -288,12 +288,32 @@ struct Spec {
   bool has_sum = false, has_max = false, has_min = false;
   std::vector<int> op_dtypes, op_modes;
   int nscal = 0;
+  // kind 6 (staged transposed operands)
+  int qd = 0, qx = 1, qxp = 1, tp = 64, rb = 1;
+  int unroll = 1;  // kind 1: vector groups per thread per trip
+  int minb = 1;    // kind 6: minimum resident CTAs per SM requested from ptxas
+  int grp = 4;     // kind 6: loop indices whose loads are issued together
+  uint32_t tmask = 0;
+  int tile_bytes = 0;
 };
 
 struct WordLayout {
   int opb, ops, outb, outs, shape, scal, redb, reds, total, psum, pmax, pmin, nsplit, chunk,
       keptn, redn, magic, nwords;
 };
+
+// symbol of each kernel class (distinct names keep profiler launch lists readable)
+static const char* kernel_name(int kind) {
+  switch (kind) {
+    case 1: return "nca_flat";
+    case 2: return "nca_nd";
+    case 3: return "nca_red_inner";
+    case 4: return "nca_red_outer";
+    case 5: return "nca_finalize";
+    case 6: return "nca_staged";
+  }
+  return "nca_kernel";
+}
 
 static WordLayout word_layout(int nops, int nd, int nscal, int nred) {
   WordLayout L;
@@ -464,6 +484,14 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
     sum_mode = ra == NCA_FLOAT32 ? 0 : ra == NCA_FLOAT64 ? 1 : 2;
   }
   os << "#define NCA_SUM_MODE " << sum_mode << "\n";
+  os << "#define NCA_UNROLL " << sp.unroll << "\n#define NCA_KNAME " << kernel_name(sp.kind) << "\n";
+  // the staged class asks for sp.minb resident CTAs per SM (register cap)
+  if (sp.kind == 6 && sp.minb > 1) os << "#define NCA_LB 256, " << sp.minb << "\n";
+  else os << "#define NCA_LB 256\n";
+  os << "#define NCA_GRP " << sp.grp << "\n";
+  os << "#define NCA_QD " << sp.qd << "\n#define NCA_QXP " << sp.qxp << "\n#define NCA_QX " << sp.qx << "\n#define NCA_TP " << sp.tp
+     << "\n#define NCA_RB " << sp.rb << "\n#define NCA_TMASK " << sp.tmask << "u\n#define NCA_TILE_BYTES "
+     << sp.tile_bytes << "\n#define NCA_NT " << __builtin_popcount(sp.tmask) << "\n";
   os << "#define NCA_W_OPB " << L.opb << "\n#define NCA_W_OPS " << L.ops << "\n#define NCA_W_OUTB " << L.outb
      << "\n#define NCA_W_OUTS " << L.outs << "\n#define NCA_W_SHAPE " << L.shape << "\n#define NCA_W_SCAL " << L.scal
      << "\n#define NCA_W_REDB " << L.redb << "\n#define NCA_W_REDS " << L.reds << "\n#define NCA_W_TOTAL " << L.total
@@ -492,6 +520,7 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
     const std::string base = "OPB_(" + std::to_string(k) + ") + off[" + std::to_string(k) + "]";
     g1 << "  v[" << k << "][0] = " << scalar_load(k, base) << ";\n";
     const int mode = sp.op_modes[k];
+    if (mode == M_STAGED) continue;   // filled from shared memory by the staged kernel
     if (mode == M_CONST || sp.vec == 1) {
       g << "  { const nca_w x = " << scalar_load(k, base) << ";";
       for (int q = 0; q < sp.vec; ++q) g << " v[" << k << "][" << q << "] = x;";
@@ -515,6 +544,10 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << g.str() << "}\n";
   os << "__device__ __forceinline__ void nca_gather1(const NcaArgs& A, const i64* off, nca_w (*v)[NCA_VEC]) {\n"
      << g1.str() << "}\n";
+  os << "#define nca_gather_ns nca_gather\n";
+  os << "__device__ __forceinline__ nca_w nca_ld_op(int k, const char* p) {\n  switch (k) {\n";
+  for (int k = 0; k < sp.nops; ++k) os << "    case " << k << ": return " << scalar_load(k, "p") << ";\n";
+  os << "  }\n  return (nca_w)0;\n}\n";
   os << "__device__ __forceinline__ nca_w nca_eval(const nca_w (*v)[NCA_VEC], int q, const u64* s, i64 lin) {\n"
      << "  (void)v; (void)q; (void)s; (void)lin;\n"
      << gen_eval(t) << "}\n";
@@ -688,6 +721,16 @@ static std::string arch_for(int dev) {
 }
 
 static std::vector<char> nvrtc_compile(const std::string& src, const std::string& arch) {
+  // NCA_JIT_DUMP=<dir> writes every generated source there (offline inspection)
+  if (const char* dump = getenv("NCA_JIT_DUMP")) {
+    if (*dump) {
+      mkdirs(dump);
+      char fn[48];
+      snprintf(fn, sizeof(fn), "/%016llx.cu", (unsigned long long)fnv1a(src));
+      std::ofstream f(std::string(dump) + fn);
+      f << src;
+    }
+  }
   nvrtcProgram prog;
   if (nvrtcCreateProgram(&prog, src.c_str(), "nca_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
     fail(NCA_ERR_COMPILE, "nvrtcCreateProgram failed");
@@ -757,6 +800,49 @@ CUfunction jit_get(const std::string& source, const char* name) {
 }
 
 // ============================================================================
+// plan cache: a compact key of everything the generated source depends on,
+// so that a launch whose kernel is known does no source generation or hashing
+// of the full text
+// ============================================================================
+static std::string plan_key(const Spec& sp, const Tape& t) {
+  std::string k;
+  k.reserve(256);
+  auto add = [&](long long v) { k += std::to_string(v); k += ','; };
+  add(sp.kind); add(sp.nops); add(sp.nd); add(sp.vec); add(sp.idx32); add(sp.nkept); add(sp.team);
+  add(sp.kept_mask); add(sp.has_out); add(sp.out_dtype); add(sp.w); add(sp.r); add(sp.nred); add(sp.red_ops);
+  add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
+  add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
+  for (int d : sp.op_dtypes) add(d);
+  k += '|';
+  for (int m : sp.op_modes) add(m);
+  k += '|';
+  for (uint32_t i : t.instrs) add(i);
+  return k;
+}
+
+static CUfunction kernel_for(const Spec& sp, const Tape& t) {
+  static std::mutex m;
+  static std::unordered_map<std::string, CUfunction> cache;
+  int dev = 0;
+  check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+  std::string key = plan_key(sp, t);
+  key += "#" + std::to_string(dev);
+  {
+    std::lock_guard<std::mutex> lk(m);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  CUfunction fn = jit_get(gen_source(sp, t), kernel_name(sp.kind));
+  if (sp.kind == 6) {
+    // the staged class lives on shared memory: ask for the largest carveout
+    check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100), "carveout");
+  }
+  std::lock_guard<std::mutex> lk(m);
+  cache[key] = fn;
+  return fn;
+}
+
+// ============================================================================
 // planning and launch
 // ============================================================================
 static void compute_magic(int64_t d, uint64_t& word) {
@@ -819,12 +905,15 @@ static void fill_common_words(const Space& s, const Spec& sp, const Tape& t, con
   w[L.total] = (uint64_t)s.total();
 }
 
-static void launch(CUfunction fn, int64_t grid, std::vector<uint64_t>& words, cudaStream_t stream) {
+static void launch(CUfunction fn, int64_t grid, std::vector<uint64_t>& words, cudaStream_t stream,
+                   unsigned smem = 0) {
   if (grid <= 0) return;
   count_launch();
   if (grid > 0x7fffffffLL) fail(NCA_ERR_LIMIT, "grid too large");
+  if (smem > 48 * 1024)
+    check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem), "smem attribute");
   void* params[] = {words.data()};
-  check_cu(drv().cuLaunchKernel(fn, (unsigned)grid, 1, 1, 256, 1, 1, 0, (CUstream)stream, params, nullptr),
+  check_cu(drv().cuLaunchKernel(fn, (unsigned)grid, 1, 1, 256, 1, 1, smem, (CUstream)stream, params, nullptr),
            "cuLaunchKernel");
 }
 
@@ -855,6 +944,124 @@ static int broadcast_shape(const nca_view* ops, int nops, int64_t* out) {
   return n;
 }
 
+
+// A kept dim q (extent <= 32) along which some operands are contiguous while
+// they are strided along p, the innermost dim: those operands are staged
+// through shared memory by kind 6. Returns q or -1.
+static int find_staged(const Space& s, uint32_t& tmask, int& nt) {
+  const int pd = s.nd - 1;
+  if (s.nd < 2 || s.red[pd]) return -1;
+  int qd = -1;
+  for (size_t k = 0; k < s.ops.size() && qd < 0; ++k) {
+    const int64_t isz = dtinfo(s.ops[k].dtype).size;
+    if (s.ops[k].st[pd] == 0 || s.ops[k].st[pd] == isz) continue;
+    for (int d = 0; d < pd; ++d)
+      if (!s.red[d] && s.ops[k].st[d] == isz && s.shape[d] <= 32) { qd = d; break; }
+  }
+  if (qd < 0) return -1;
+  tmask = 0;
+  nt = 0;
+  for (size_t k = 0; k < s.ops.size(); ++k) {
+    const int64_t isz = dtinfo(s.ops[k].dtype).size;
+    if (s.ops[k].st[qd] == isz && s.ops[k].st[pd] != isz && s.ops[k].st[pd] != 0) { tmask |= 1u << k; ++nt; }
+  }
+  return qd;
+}
+
+// Launches kind 6 (and its finalize when the loop dims are split). Kept dims
+// are those with s.red false; KN / RN are the kept / loop element counts.
+static void launch_staged(const Space& s, Spec sp, const Tape& tape, int qd, uint32_t tmask, int nt, int64_t KN,
+                          int64_t RN, cudaStream_t stream) {
+  const int sms = sm_count(current_device());
+  const int pd = s.nd - 1;
+  const int64_t P = s.shape[pd], QX = s.shape[qd];
+  const int wsz = dtinfo(sp.w).size;
+  sp.nd = s.nd;
+  sp.kind = 6;
+  {
+    // resident CTAs per SM asked of ptxas (NCA_STAGED_MINB overrides; 2 caps
+    // registers at 128 and measured fastest with groups of 4 loop indices)
+    static const int minb = [] {
+      const char* e = getenv("NCA_STAGED_MINB");
+      const int v = e ? atoi(e) : 0;
+      return v >= 1 && v <= 8 ? v : 2;
+    }();
+    sp.minb = minb;
+    static const int grp = [] {
+      const char* e = getenv("NCA_STAGED_GRP");
+      const int v = e ? atoi(e) : 0;
+      return v == 1 || v == 2 || v == 4 || v == 8 ? v : 4;
+    }();
+    sp.grp = grp;
+  }
+  // 4-wide vectors along p for the other operands and the stored value when
+  // they are contiguous and aligned there (plan_vec), else scalars
+  plan_vec(s, sp, 4, sp.has_out);
+  for (int k = 0; k < sp.nops; ++k) if ((tmask >> k) & 1u) sp.op_modes[k] = M_STAGED;
+  sp.kept_mask = 0;
+  for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
+  sp.qd = qd;
+  sp.qx = (int)QX;
+  sp.qxp = 1;
+  while (sp.qxp < QX) sp.qxp *= 2;
+  sp.tmask = tmask;
+  // rb: power of two with qxp * rb <= 256; tp a multiple of 256 / (qxp * rb)
+  // with at most 32 staged registers per thread and operand
+  // tile of tp p values (a multiple of vec); rb: power of two with qxp * rb
+  // <= 256 and at most 16 staged registers per thread over all staged operands
+  sp.tp = P > 32 ? 64 : 32;
+  sp.rb = std::max(1, std::min(16, 256 / sp.qxp));
+  while (sp.rb > 1 && (int64_t)sp.tp * sp.qxp * sp.rb / 256 * nt > 16) sp.rb /= 2;
+  const int64_t budget = 40 * 1024 / (int64_t)(nt * sp.tp * wsz);
+  while (sp.rb > 1 && (int64_t)sp.rb * QX + 1 > budget) sp.rb /= 2;
+  const int pstep = 256 / (sp.qxp * sp.rb);
+  if (sp.tp < pstep) sp.tp = pstep;
+  sp.tile_bytes = (int)(((int64_t)nt * sp.tp * (sp.rb * QX + 1) * wsz + 15) / 16 * 16);
+  const int64_t ptiles = cdiv(P, sp.tp);
+  const int64_t units = (KN / (P * QX)) * ptiles;
+  const unsigned smem = (unsigned)(sp.tile_bytes + 2 * (sp.nops + 1) * sp.rb * 8);
+  CUfunction fn = kernel_for(sp, tape);
+  // split the loop dims so the grid fills whole waves of resident CTAs
+  int per_sm = 1;
+  if (drv().cuOccupancyMaxActiveBlocksPerMultiprocessor)
+    check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem), "occupancy");
+  const int64_t wave = (int64_t)sms * std::max(per_sm, 1);
+  int64_t S = 1;
+  if (RN > 0) {
+    const int64_t smax = cdiv(RN, sp.rb);
+    if (units < wave) S = std::min<int64_t>(cdiv(wave, units), smax);
+    // round the CTA count up to whole waves when the loop dims allow it
+    const int64_t ctas = units * S;
+    if (ctas > wave && ctas % wave != 0) {
+      const int64_t want = cdiv(ctas, wave) * wave;
+      if (want % units == 0 && want / units <= smax) S = want / units;
+    }
+  }
+  int64_t C = RN > 0 ? cdiv(cdiv(RN, S), sp.rb) * sp.rb : 0;
+  if (C > 0) S = cdiv(RN, C);
+  if (S < 1) S = 1;
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  std::vector<uint64_t> w;
+  fill_common_words(s, sp, tape, L, w);
+  w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+  const bool split = S > 1 && sp.nred > 0;
+  StreamScratch part(split ? (size_t)(S * KN) * 8 * ((sp.has_sum ? 1 : 0) + (sp.has_max ? 2 : 0) + (sp.has_min ? 2 : 0)) : 0,
+                     stream);
+  if (split) {
+    uint64_t* p = (uint64_t*)part.ptr;
+    if (sp.has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
+    if (sp.has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+    if (sp.has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+  }
+  launch(fn, units * S, w, stream, smem);
+  if (split) {
+    Spec fs = sp;
+    fs.kind = 5;
+    CUfunction ff = kernel_for(fs, tape);
+    launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
+  }
+}
+
 void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& out, cudaStream_t stream) {
   check_view(out, "out");
   if (nops < 0 || nops > NCA_MAX_OPERANDS) fail(NCA_ERR_LIMIT, "%d operands (0..%d)", nops, NCA_MAX_OPERANDS);
@@ -878,6 +1085,23 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
   sp.nops = nops; sp.nd = s.nd; sp.has_out = true; sp.out_dtype = out.dtype; sp.w = tape.compute_dtype;
   sp.r = tape.result_dtype; sp.nscal = (int)tape.scalar_dtypes.size();
   for (int k = 0; k < nops; ++k) sp.op_dtypes.push_back(ops[k].dtype);
+  // transposed operands: stage them (kind 6) with p and q kept and every other
+  // dim walked as a loop dim; the output must be contiguous along p
+  if (!tape.uses_idx && s.nd >= 2 && s.out.st[s.nd - 1] == dtinfo(out.dtype).size) {
+    uint32_t tmask = 0;
+    int nt = 0;
+    const int qd = find_staged(s, tmask, nt);
+    if (qd >= 0) {
+      Space t = s;
+      int64_t KN = 1, RN = 1;
+      for (int d = 0; d < t.nd; ++d) {
+        t.red[d] = !(d == qd || d == t.nd - 1);
+        if (t.red[d]) RN *= t.shape[d]; else KN *= t.shape[d];
+      }
+      launch_staged(t, sp, tape, qd, tmask, nt, KN, RN, stream);
+      return;
+    }
+  }
   bool flat = s.nd == 1 && s.out.st[0] == dtinfo(out.dtype).size;
   for (int k = 0; k < nops && flat; ++k)
     if (s.ops[k].st[0] != 0 && s.ops[k].st[0] != dtinfo(ops[k].dtype).size) flat = false;
@@ -886,6 +1110,7 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
     for (int k = 0; k < nops; ++k) if (sp.op_modes[k] == M_STRIDED && sp.vec > 1) flat = false;
   }
   sp.kind = flat ? 1 : 2;
+  sp.unroll = flat ? (nops <= 2 ? 4 : nops <= 4 ? 2 : 1) : 1;
   const int64_t total = s.total();
   bool small_dims = true;
   for (int d = 0; d < s.nd; ++d) if (s.shape[d] >= (1ll << 31)) small_dims = false;
@@ -898,10 +1123,11 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
     if (d == s.nd - 1) dv /= sp.vec;
     compute_magic(dv, w[L.magic + d]);
   }
-  CUfunction fn = jit_get(gen_source(sp, tape), "nca_kernel");
+  CUfunction fn = kernel_for(sp, tape);
   const int dev = current_device();
   const int64_t groups = total / sp.vec;
-  int64_t grid = std::min<int64_t>(cdiv(std::max<int64_t>(groups, 1), 256), (int64_t)sm_count(dev) * 16);
+  int64_t grid = std::min<int64_t>(cdiv(std::max<int64_t>(groups, 1), 256 * (int64_t)sp.unroll),
+                                   (int64_t)sm_count(dev) * 8);
   launch(fn, grid, w, stream);
 }
 
@@ -1019,18 +1245,29 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
       if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
     }
-    CUfunction fn = jit_get(gen_source(sp, tape), "nca_kernel");
+    CUfunction fn = kernel_for(sp, tape);
     launch(fn, cdiv(KN * S, tpb), w, stream);
     if (S > 1) {
       Spec fs = sp; fs.kind = 5;
-      CUfunction ff = jit_get(gen_source(fs, tape), "nca_kernel");
+      CUfunction ff = kernel_for(fs, tape);
       launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
     }
     return;
   }
-  // innermost dim kept: RED_OUTER
+  // innermost dim kept. Operands strided along it but contiguous along another
+  // kept dim q are staged through shared memory (kind 6); otherwise RED_OUTER.
   sp.nd = s.nd;
+  {
+    uint32_t tmask = 0;
+    int nt = 0;
+    const int qd = tape.uses_idx ? -1 : find_staged(s, tmask, nt);
+    if (qd >= 0) {
+      launch_staged(s, sp, tape, qd, tmask, nt, KN, RN, stream);
+      return;
+    }
+  }
   sp.kind = 4;
+  sp.kept_mask = 0;
   for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
   plan_vec(s, sp, 4, out != nullptr);
   const int64_t KG = KN / sp.vec;
@@ -1050,11 +1287,11 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
     if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
   }
-  CUfunction fn = jit_get(gen_source(sp, tape), "nca_kernel");
+  CUfunction fn = kernel_for(sp, tape);
   launch(fn, cdiv(KG * S, 256), w, stream);
   if (S > 1) {
     Spec fs = sp; fs.kind = 5;
-    CUfunction ff = jit_get(gen_source(fs, tape), "nca_kernel");
+    CUfunction ff = kernel_for(fs, tape);
     launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
   }
 }
@@ -1103,6 +1340,21 @@ int jit_selftest(const char* arch) {
       nvrtc_compile(src, a);
       ++n;
     }
+    // kind 6: operand 0 staged through shared memory, dims (q, b, r, p)
+    Spec sp;
+    sp.kind = 6; sp.nops = 3; sp.nd = 4; sp.vec = 1; sp.w = d[0]; sp.r = d[1]; sp.out_dtype = d[1]; sp.nscal = 1;
+    sp.op_dtypes = {d[2], d[2], d[2]};
+    sp.op_modes = {M_STAGED, M_CONTIG, M_CONST};
+    sp.vec = std::min(d[3], 4);
+    sp.has_out = true; sp.nred = 2; sp.red_ops = 2u | (4u << 4); sp.has_max = true;
+    sp.kept_mask = 1u | 2u | 8u; sp.qd = 0; sp.qx = 8; sp.qxp = 8; sp.tmask = 1u; sp.tp = 64; sp.rb = 8; sp.minb = 3;
+    sp.tile_bytes = 64 * (8 * 8 + 1) * dtinfo(d[0]).size;
+    nvrtc_compile(gen_source(sp, t), a);
+    ++n;
+    // kind 6 without reductions (a transposed elementwise expression)
+    sp.nred = 0; sp.red_ops = 0; sp.has_max = false; sp.kept_mask = 1u | 8u;
+    nvrtc_compile(gen_source(sp, t), a);
+    ++n;
   }
   return n;
 }

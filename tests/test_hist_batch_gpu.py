@@ -44,6 +44,74 @@ def test_hist2d_matches_oracle(cuda, orc, n, nb):
     assert np.array_equal(c2.to_host().reshape(-1), rc)
 
 
+def _check_hist(x, y, w, nbx, nby, orc, xr=(0.0, 1.0), yr=(0.0, 1.0)):
+    counts, wsum = hist2d(nca.NCDevArray.from_host(x), nca.NCDevArray.from_host(y), nbx, nby, xr, yr,
+                          w=nca.NCDevArray.from_host(w))
+    rc, rw = orc.hist2d(x, y, w, nbx, nby, xr[0], xr[1], yr[0], yr[1])
+    assert np.array_equal(counts.to_host().reshape(-1), rc)
+    got = wsum.to_host().reshape(-1).astype(np.float64)
+    ref32 = rw.astype(np.float32).astype(np.float64)
+    assert np.all(np.abs(got - ref32) <= 2.0**-23 * np.abs(rw) + 1e-30)
+    return rc, rw
+
+
+def test_hist2d_bucket_overflow(cuda, orc):
+    """The sampled blocks (every 32nd block of 1024 points) spread over the
+    grid while all other points crowd into one tile: that tile's bucket
+    overflows and its excess goes through the direct atomics."""
+    rng = np.random.default_rng(SEED + 6)
+    n = (1 << 21) + 777
+    x = rng.uniform(0.40, 0.41, n).astype(np.float32)
+    y = rng.uniform(0.50, 0.505, n).astype(np.float32)
+    idx = np.arange(n)
+    sampled = (idx // 1024) % 32 == 0
+    x[sampled] = rng.uniform(0, 1, sampled.sum()).astype(np.float32)
+    y[sampled] = rng.uniform(0, 1, sampled.sum()).astype(np.float32)
+    w = rng.lognormal(0, 1, n).astype(np.float32)
+    _check_hist(x, y, w, 1024, 1024, orc)
+
+
+def test_hist2d_partial_tile_and_ranges(cuda, orc):
+    """A grid that is not a whole number of 16384-bin tiles, a range other
+    than [0,1)^2, and points outside it."""
+    rng = np.random.default_rng(SEED + 7)
+    n = (1 << 20) + 12345
+    x = rng.normal(0.0, 2.0, n).astype(np.float32)
+    y = rng.normal(1.0, 3.0, n).astype(np.float32)
+    w = rng.lognormal(0, 1, n).astype(np.float32)
+    _check_hist(x, y, w, 1000, 1100, orc, xr=(-4.0, 4.0), yr=(-5.0, 7.0))
+
+
+def test_hist2d_single_bin(cuda, orc):
+    """Every point in one bin (maximal collisions)."""
+    n = 1 << 21
+    rng = np.random.default_rng(SEED + 8)
+    x = np.full(n, 0.5, np.float32)
+    y = np.full(n, 0.25, np.float32)
+    w = rng.lognormal(0, 1, n).astype(np.float32)
+    _check_hist(x, y, w, 512, 512, orc)
+
+
+def test_hist2d_accumulates_and_empty(cuda, orc):
+    from ncarray_gb300.hist import hist2d_into
+    rng = np.random.default_rng(SEED + 9)
+    x, y = mixture_points(rng, 1 << 20)
+    w = rng.lognormal(0, 1, x.size).astype(np.float32)
+    dx, dy, dw = (nca.NCDevArray.from_host(a) for a in (x, y, w))
+    counts = nca.NCDevArray((256, 256), nca.DType.uint64).fill(0)
+    wsum = nca.NCDevArray((256, 256), nca.DType.float32).fill(0.0)
+    hist2d_into(dx, dy, counts, (0.0, 1.0), (0.0, 1.0), dw, wsum)
+    hist2d_into(dx, dy, counts, (0.0, 1.0), (0.0, 1.0), dw, wsum)
+    rc, rw = orc.hist2d(x, y, w, 256, 256, 0.0, 1.0, 0.0, 1.0)
+    assert np.array_equal(counts.to_host().reshape(-1), 2 * rc)
+    got = wsum.to_host().reshape(-1).astype(np.float64)
+    assert np.all(np.abs(got - 2 * rw) <= 2.0**-22 * np.abs(rw) + 1e-30)
+    # no points: outputs unchanged
+    e = nca.NCDevArray((0,), nca.DType.float32)
+    hist2d_into(e, e, counts, (0.0, 1.0), (0.0, 1.0))
+    assert np.array_equal(counts.to_host().reshape(-1), 2 * rc)
+
+
 def make_batch(rng, n, lo=64, hi=1 << 16):
     lens = np.round(np.exp(rng.uniform(np.log(lo), np.log(hi), n))).astype(np.int64)
     lens[:3] = [1, 64, 257][: min(n, 3)]
