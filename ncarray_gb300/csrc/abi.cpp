@@ -10,6 +10,7 @@ using namespace nca;
 
 namespace nca {
 int stencil_read_status(cudaStream_t s);
+int hist_read_status(cudaStream_t s);
 }
 
 extern "C" {
@@ -23,7 +24,9 @@ int64_t nca_launch_count(void) { return launch_count(); }
 int32_t nca_device_status(int32_t* status, void* stream) {
   return guarded([&] {
     if (!status) fail(NCA_ERR_INVALID, "null status");
-    *status = stencil_read_status((cudaStream_t)stream);
+    const int st = stencil_read_status((cudaStream_t)stream);
+    const int hs = hist_read_status((cudaStream_t)stream);
+    *status = st != 0 ? st : hs;
   });
 }
 

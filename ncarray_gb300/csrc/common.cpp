@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <atomic>
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 namespace nca {
@@ -141,9 +142,32 @@ int sm_count(int dev) {
   return cache[dev];
 }
 
+// One stream-ordered memory pool per device owned by the library. Its
+// release threshold is unbounded, so memory freed at the end of a call stays
+// mapped for the next one instead of being returned to the driver at every
+// synchronisation (remapping a gigabyte of scratch costs about a millisecond).
+static cudaMemPool_t scratch_pool(int dev) {
+  static std::mutex mu;
+  static std::vector<cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  if ((int)pools.size() <= dev) pools.resize(dev + 1, nullptr);
+  if (!pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    check_cuda(cudaMemPoolCreate(&p, &props), "cudaMemPoolCreate");
+    uint64_t threshold = ~0ull;
+    check_cuda(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &threshold), "pool release threshold");
+    pools[dev] = p;
+  }
+  return pools[dev];
+}
+
 StreamScratch::StreamScratch(size_t bytes, cudaStream_t s) : stream(s) {
   if (bytes == 0) return;
-  cudaError_t e = cudaMallocAsync(&ptr, bytes, s);
+  cudaError_t e = cudaMallocFromPoolAsync(&ptr, bytes, scratch_pool(current_device()), s);
   if (e != cudaSuccess) {
     ptr = nullptr;
     check_cuda(e, "cudaMallocAsync(scratch)");

@@ -18,10 +18,11 @@
 //      in each tile of TB consecutive bins; each tile gets a bucket with 25 %
 //      slack (the total is bounded, so the scratch is sized on the host);
 //   2. scatter: every CTA bins a chunk of points, ranks them per tile with
-//      warp-aggregated shared-memory atomics and appends (bin within tile:
-//      uint16, weight: float32) records to the tile buckets (one global atomic
-//      per tile and CTA); records that do not fit in their bucket are added
-//      with global atomics directly;
+//      shared-memory atomics, orders the chunk's (bin within tile: uint16,
+//      weight: float32) records by tile in shared memory and appends each
+//      tile's run to its bucket with coalesced stores (one global atomic per
+//      tile and CTA reserves the space); records that do not fit in their
+//      bucket are added with global atomics directly;
 //   3. accumulate: a persistent grid splits the concatenated buckets into
 //      equal record ranges; a CTA counts each tile piece of its range into a
 //      shared-memory copy of the tile (uint32 counts, float32 sums and
@@ -41,11 +42,23 @@ namespace {
 
 constexpr int THREADS = 256;
 constexpr int TB = 16384;               // bins per tile (local index fits in uint16)
-constexpr int MAX_TILES = 256;          // partitioned path limit (4 Mi bins)
+constexpr int MAX_TILES = 256;          // partitioned path limit (4 Mi bins; tile index fits in uint8)
 constexpr int SAMPLE = 32;              // 1 block of 1024 points in SAMPLE is counted in pass 1
-constexpr int CHUNK = 4096;             // points per CTA in the scatter pass
+constexpr int CHUNK = 2048;             // points per chunk in the scatter pass
 constexpr int PER_THREAD = CHUNK / THREADS;
+static_assert(MAX_TILES == THREADS, "the scatter pass scans one tile count per thread");
 constexpr int ACC_THREADS = 1024;
+constexpr int NSUB = 1;                 // sub-buckets per tile (by scatter CTA index)
+constexpr int SCAN_THREADS = 1024;      // one-block scans over <= 4 * SCAN_THREADS buckets
+constexpr int SLACK = 2048;             // records of slack per bucket
+constexpr int FPAD = 16;                // fill counters 128 bytes apart (uint64)
+constexpr int EPAD = 32;                // estimate counters 128 bytes apart (uint32)
+static_assert(MAX_TILES * NSUB <= 4 * SCAN_THREADS, "bucket scan size");
+
+constexpr unsigned OVERFLOW = 0x80000000u;   // staged record that did not fit its bucket
+constexpr unsigned long long kWaitNs = 2000000000ull;   // bound of every mbarrier wait
+
+static __device__ int g_hist_status;   // NCA_ERR_TIMEOUT after a wait that ran out
 
 struct Bins {
   float xl, yl, sx, sy, fnx, fny;
@@ -80,18 +93,36 @@ __global__ void __launch_bounds__(THREADS) wsum_finish_kernel(const double* __re
     wsum[i] = __double2float_rn((double)wsum[i] + wacc[i]);
 }
 
-// inclusive prefix sum of MAX_TILES values held one per thread
-__device__ __forceinline__ long long block_scan(long long v, long long* sc) {
+// Exclusive prefix sums of n <= SCAN_THREADS * 4 values v(i) by one block of
+// SCAN_THREADS threads: out[i] for i < n and out[n] = total.
+template <class F>
+__device__ __forceinline__ void block_scan(int n, F v, long long* __restrict__ out) {
+  __shared__ long long sc[SCAN_THREADS];
   const int t = threadIdx.x;
-  sc[t] = v;
+  long long a[4];
+  long long sum = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = t * 4 + j;
+    a[j] = i < n ? v(i) : 0;
+    sum += a[j];
+  }
+  sc[t] = sum;
   __syncthreads();
-  for (int d = 1; d < MAX_TILES; d <<= 1) {
+  for (int d = 1; d < SCAN_THREADS; d <<= 1) {
     const long long u = t >= d ? sc[t - d] : 0;
     __syncthreads();
     sc[t] += u;
     __syncthreads();
   }
-  return sc[t];
+  long long run = sc[t] - sum;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int i = t * 4 + j;
+    if (i < n) out[i] = run;
+    run += a[j];
+  }
+  if (t == SCAN_THREADS - 1) out[n] = sc[t];
 }
 
 // ---- pass 1: sampled tile counts -------------------------------------------------
@@ -112,117 +143,222 @@ tile_sample_kernel(const float* __restrict__ x, const float* __restrict__ y, lon
   }
   __syncthreads();
   for (int t = threadIdx.x; t < ntiles; t += THREADS)
-    if (cnt[t]) atomicAdd(est + t, cnt[t]);
+    if (cnt[t]) atomicAdd(est + (long long)t * EPAD, cnt[t]);
 }
 
-// bucket capacity and offset of every tile; capacities are multiples of 8
-// records so that every bucket starts 16-byte aligned
-__global__ void __launch_bounds__(MAX_TILES)
-tile_plan_kernel(const unsigned* __restrict__ est, int ntiles, long long* __restrict__ off,
+__device__ __forceinline__ long long bucket_cap(const unsigned* __restrict__ est, int v) {
+  const long long e = est[(long long)(v / NSUB) * EPAD];
+  return ((e * (SAMPLE * 5 / 4) / NSUB + 7) & ~7ll) + SLACK;
+}
+
+// capacity and offset of every bucket (tile t, sub-bucket u) = t * NSUB + u;
+// capacities are multiples of 8 records so every bucket starts 16-byte aligned
+__global__ void __launch_bounds__(SCAN_THREADS)
+tile_plan_kernel(const unsigned* __restrict__ est, int nv, long long* __restrict__ off,
                  long long* __restrict__ cap, unsigned long long* __restrict__ fill) {
-  __shared__ long long sc[MAX_TILES];
-  const int t = threadIdx.x;
-  const long long c = t < ntiles ? (long long)est[t] * (SAMPLE * 5 / 4) + 4096 : 0;
-  const long long inc = block_scan(c, sc);
-  if (t < ntiles) {
-    off[t] = inc - c;
-    cap[t] = c;
-    fill[t] = 0;
+  block_scan(nv, [&](int v) { return bucket_cap(est, v); }, off);
+  for (int v = threadIdx.x; v < nv; v += SCAN_THREADS) {
+    cap[v] = bucket_cap(est, v);
+    fill[(long long)v * FPAD] = 0;
   }
-  if (t == ntiles - 1) off[ntiles] = inc;
 }
 
-// ---- pass 2: scatter points into tile buckets -------------------------------------
+// ---- pass 2: scatter points into buckets ------------------------------------------
+// A persistent grid walks the chunks of CHUNK points; the next chunk of x, y
+// (and w) is fetched by bulk copies into the other half of a double buffer
+// while the current one is binned. Waits are bounded (2 s of %globaltimer):
+// on a timeout the CTA records NCA_ERR_TIMEOUT, waits for its copies in
+// flight and stops. CTA c appends to sub-bucket c % NSUB of every tile.
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    if (ok) return true;
+    if (gtimer() - t0 > limit_ns) return false;
+  }
+}
+
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+
 template <bool WEIGHTED>
-__global__ void __launch_bounds__(THREADS)
+__host__ __device__ constexpr int scatter_smem() {
+  return 2 * (WEIGHTED ? 3 : 2) * CHUNK * 4 + 16;
+}
+
+template <bool WEIGHTED>
+__global__ void __launch_bounds__(THREADS, 3)
 tile_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ w,
                     long long n, Bins B, int ntiles, const long long* __restrict__ off,
                     const long long* __restrict__ cap, unsigned long long* __restrict__ fill,
                     unsigned short* __restrict__ rec_bin, float* __restrict__ rec_w,
                     unsigned long long* __restrict__ counts, double* __restrict__ wacc) {
+  constexpr int NA = WEIGHTED ? 3 : 2;              // arrays fetched per chunk
+  constexpr uint32_t ABYTES = CHUNK * 4;
+  extern __shared__ __align__(128) unsigned char sm[];
+  const float* buf = reinterpret_cast<const float*>(sm);   // [2][NA][CHUNK]
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+  const uint32_t bbase = sbase + 2 * NA * ABYTES;          // two mbarriers
   __shared__ unsigned cnt[MAX_TILES];
-  __shared__ long long base[MAX_TILES];   // start of this CTA's run in the bucket
-  __shared__ unsigned avail[MAX_TILES];   // how many of the run fit in the bucket
-  const long long c0 = (long long)blockIdx.x * CHUNK;
-  if (c0 >= n) return;
-  for (int t = threadIdx.x; t < ntiles; t += THREADS) cnt[t] = 0;
-  __syncthreads();
-  int bins[PER_THREAD];
-  float ws[PER_THREAD];
-#pragma unroll
-  for (int k = 0; k < PER_THREAD; ++k) {
-    const long long i = c0 + threadIdx.x + (long long)k * THREADS;
-    bins[k] = -1;
-    ws[k] = 0.f;
-    if (i < n) {
-      bins[k] = bin_of(B, __ldcs(x + i), __ldcs(y + i));
-      if (WEIGHTED) ws[k] = __ldcs(w + i);
-    }
-  }
-  // rank within the CTA's run of the tile: one shared atomic per distinct tile in the warp
-  const unsigned lane = threadIdx.x & 31u;
-  unsigned rank[PER_THREAD];
-#pragma unroll
-  for (int k = 0; k < PER_THREAD; ++k) {
-    const int t = bins[k] >= 0 ? bins[k] / TB : -1;
-    const unsigned m = __match_any_sync(0xffffffffu, t);
-    const int leader = __ffs(m) - 1;
-    unsigned r0 = 0;
-    if ((int)lane == leader && t >= 0) r0 = atomicAdd(&cnt[t], (unsigned)__popc(m));
-    r0 = __shfl_sync(0xffffffffu, r0, leader);
-    rank[k] = r0 + (unsigned)__popc(m & ((1u << lane) - 1u));
+  __shared__ unsigned loff[MAX_TILES];      // start of each tile's run in the staged chunk
+  __shared__ unsigned wpre[THREADS / 32];
+  __shared__ unsigned base[MAX_TILES];      // start of this CTA's run in the record arrays
+  __shared__ unsigned avail[MAX_TILES];     // how many of the run fit in the bucket
+  __shared__ unsigned short sbin[CHUNK];    // the chunk's records ordered by tile
+  __shared__ float sw[WEIGHTED ? CHUNK : 1];
+  __shared__ unsigned sdst[CHUNK];          // record index, or OVERFLOW | tile
+  const long long nfull = n / CHUNK, nchunks = (n + CHUNK - 1) / CHUNK;
+  const int sub = (int)(blockIdx.x % NSUB);
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bbase) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bbase + 8) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < ntiles; t += THREADS) {
-    base[t] = 0;
-    avail[t] = 0;
-    if (cnt[t]) {
-      // positions [p, p + cnt) are this CTA's; the part below the capacity is
-      // always written, so every position below min(fill, cap) holds a record
-      const unsigned long long p = atomicAdd(fill + t, (unsigned long long)cnt[t]);
-      const long long room = cap[t] - (long long)p;
-      base[t] = off[t] + (long long)p;
-      avail[t] = room <= 0 ? 0u : (room >= (long long)cnt[t] ? cnt[t] : (unsigned)room);
-    }
-  }
-  __syncthreads();
+  auto issue = [&](long long ch, int b) {
+    const uint32_t bar = bbase + 8 * b, dst = sbase + (uint32_t)(b * NA) * ABYTES;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(NA * ABYTES) : "memory");
+    bulk_load(dst, x + ch * CHUNK, ABYTES, bar);
+    bulk_load(dst + ABYTES, y + ch * CHUNK, ABYTES, bar);
+    if (WEIGHTED) bulk_load(dst + 2 * ABYTES, w + ch * CHUNK, ABYTES, bar);
+  };
+  long long ch = blockIdx.x;
+  if (threadIdx.x == 0 && ch < nfull) issue(ch, 0);
+  int it = 0;
+  bool failed = false;
+  for (; ch < nchunks; ch += gridDim.x, ++it) {
+    const int b = it & 1;
+    const long long nxt = ch + gridDim.x;
+    // buffer b ^ 1 was released by the barrier that ended the previous iteration
+    if (threadIdx.x == 0 && nxt < nfull) issue(nxt, b ^ 1);
+    for (int t = threadIdx.x; t < ntiles; t += THREADS) cnt[t] = 0;
+    const bool full = ch < nfull;
+    const bool ok = !full || mbar_wait(bbase + 8 * b, (uint32_t)((it >> 1) & 1), kWaitNs);
+    if (__syncthreads_or(ok ? 0 : 1)) { failed = true; break; }
+    const long long c0 = ch * CHUNK;
+    const float* bx = buf + (size_t)(b * NA) * CHUNK;
+    int bins[PER_THREAD];
+    float ws[PER_THREAD];
 #pragma unroll
-  for (int k = 0; k < PER_THREAD; ++k) {
-    const int b = bins[k];
-    if (b < 0) continue;
-    const int t = b / TB;
-    if (rank[k] < avail[t]) {
-      const long long bs = base[t];
-      rec_bin[bs + rank[k]] = (unsigned short)(b - t * TB);
-      if (WEIGHTED) rec_w[bs + rank[k]] = ws[k];
-    } else {
-      atomicAdd(counts + b, 1ull);
-      if (WEIGHTED) atomicAdd(wacc + b, (double)ws[k]);
+    for (int k = 0; k < PER_THREAD; ++k) {
+      const int li = threadIdx.x + k * THREADS;
+      bins[k] = -1;
+      ws[k] = 0.f;
+      if (full) {
+        bins[k] = bin_of(B, bx[li], bx[CHUNK + li]);
+        if (WEIGHTED) ws[k] = bx[2 * CHUNK + li];
+      } else if (c0 + li < n) {
+        bins[k] = bin_of(B, __ldcs(x + c0 + li), __ldcs(y + c0 + li));
+        if (WEIGHTED) ws[k] = __ldcs(w + c0 + li);
+      }
     }
+    // rank within the CTA's run of the tile (lanes of a warp on the same
+    // counter are serialised by the shared-memory unit, one issue slot each)
+    unsigned rank[PER_THREAD];
+#pragma unroll
+    for (int k = 0; k < PER_THREAD; ++k) rank[k] = bins[k] >= 0 ? atomicAdd(&cnt[bins[k] / TB], 1u) : 0u;
+    __syncthreads();
+    // exclusive scan of the tile counts (ntiles <= MAX_TILES == THREADS)
+    {
+      const int t = threadIdx.x, lane = t & 31, wp = t >> 5;
+      const unsigned v0 = t < ntiles ? cnt[t] : 0u;
+      unsigned v = v0;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const unsigned u = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += u;
+      }
+      if (lane == 31) wpre[wp] = v;
+      __syncthreads();
+      if (wp == 0) {
+        unsigned q = lane < THREADS / 32 ? wpre[lane] : 0u;
+        const unsigned q0 = q;
+#pragma unroll
+        for (int d = 1; d < THREADS / 32; d <<= 1) {
+          const unsigned u = __shfl_up_sync(0xffffffffu, q, d);
+          if (lane >= d) q += u;
+        }
+        if (lane < THREADS / 32) wpre[lane] = q - q0;
+      }
+      __syncthreads();
+      loff[t] = v - v0 + wpre[wp];
+    }
+    for (int t = threadIdx.x; t < ntiles; t += THREADS) {
+      base[t] = 0;
+      avail[t] = 0;
+      if (cnt[t]) {
+        // positions [p, p + cnt) are this CTA's; the part below the capacity is
+        // always written, so every position below min(fill, cap) holds a record
+        const int v = t * NSUB + sub;
+        const unsigned long long p = atomicAdd(fill + (long long)v * FPAD, (unsigned long long)cnt[t]);
+        const long long room = cap[v] - (long long)p;
+        base[t] = (unsigned)(off[v] + (long long)p);
+        avail[t] = room <= 0 ? 0u : (room >= (long long)cnt[t] ? cnt[t] : (unsigned)room);
+      }
+    }
+    __syncthreads();
+    // stage the records in tile order with their destinations
+#pragma unroll
+    for (int k = 0; k < PER_THREAD; ++k) {
+      const int bn = bins[k];
+      if (bn < 0) continue;
+      const int t = bn / TB;
+      const unsigned j = loff[t] + rank[k];
+      sbin[j] = (unsigned short)(bn - t * TB);
+      sdst[j] = rank[k] < avail[t] ? base[t] + rank[k] : (OVERFLOW | (unsigned)t);
+      if (WEIGHTED) sw[j] = ws[k];
+    }
+    __syncthreads();
+    // consecutive threads write consecutive records of a tile's run
+    const unsigned total = loff[ntiles - 1] + cnt[ntiles - 1];
+    for (unsigned j = threadIdx.x; j < total; j += THREADS) {
+      const unsigned d = sdst[j];
+      if (!(d & OVERFLOW)) {
+        rec_bin[d] = sbin[j];
+        if (WEIGHTED) rec_w[d] = sw[j];
+      } else {
+        const long long bn = (long long)(d & ~OVERFLOW) * TB + sbin[j];
+        atomicAdd(counts + bn, 1ull);
+        if (WEIGHTED) atomicAdd(wacc + bn, (double)sw[j]);
+      }
+    }
+    __syncthreads();
+  }
+  if (failed && threadIdx.x == 0) {
+    atomicExch(&g_hist_status, (int)NCA_ERR_TIMEOUT);
+    // copies in flight: buffer it & 1 (this chunk) and the prefetch of the next
+    const int b = it & 1;
+    if (ch < nfull) mbar_wait(bbase + 8 * b, (uint32_t)((it >> 1) & 1), kWaitNs / 2);
+    if (ch + gridDim.x < nfull) mbar_wait(bbase + 8 * (b ^ 1), (uint32_t)(((it + 1) >> 1) & 1), kWaitNs / 2);
   }
 }
 
-// stored records per tile and their exclusive prefix sum P (P[ntiles] = total)
-__global__ void __launch_bounds__(MAX_TILES)
-tile_prefix_kernel(int ntiles, const long long* __restrict__ cap, const unsigned long long* __restrict__ fill,
-                   long long* __restrict__ P) {
-  __shared__ long long sc[MAX_TILES];
-  const int t = threadIdx.x;
-  long long f = 0;
-  if (t < ntiles) {
-    const long long ft = (long long)fill[t];
-    f = ft < cap[t] ? ft : cap[t];
-  }
-  const long long inc = block_scan(f, sc);
-  if (t < ntiles) P[t] = inc - f;
-  if (t == ntiles - 1) P[ntiles] = inc;
+// stored records per bucket and their exclusive prefix sum PV (PV[nv] = total)
+__global__ void __launch_bounds__(SCAN_THREADS)
+tile_prefix_kernel(int nv, const long long* __restrict__ cap, const unsigned long long* __restrict__ fill,
+                   long long* __restrict__ PV) {
+  block_scan(nv, [&](int v) {
+    const long long ft = (long long)fill[(long long)v * FPAD];
+    return ft < cap[v] ? ft : cap[v];
+  }, PV);
 }
 
 // ---- pass 3: per-tile shared-memory histograms of record ranges -------------------
 // CTA g takes records [R g / G, R (g + 1) / G) of the concatenated buckets
-// (tile t holds positions [P[t], P[t+1])); its piece of tile t is stored in
-// partial slot g + t, which is unique because both g and t grow along the
-// concatenation.
+// (bucket v holds positions [PV[v], PV[v+1]), tile t the buckets t * NSUB ..
+// t * NSUB + NSUB - 1); its piece of tile t is stored in partial slot g + t,
+// which is unique because both g and t grow along the concatenation.
 __device__ __forceinline__ long long range_start(long long R, int g, int G) { return R * g / G; }
 
 template <bool WEIGHTED>
@@ -250,60 +386,72 @@ __device__ __forceinline__ void acc_vec(unsigned* c, float* s, float* e, uint4 q
 }
 
 template <bool WEIGHTED>
+__device__ __forceinline__ void acc_range(unsigned* c, float* s, float* e, const unsigned short* __restrict__ rec_bin,
+                                          const float* __restrict__ rec_w, long long a, long long b) {
+  // records [a, b) of the record arrays; bucket starts are multiples of 8
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  long long a8 = (a + 7) & ~7ll;
+  if (a8 > b) a8 = b;
+  const long long nv = (b - a8) >> 3, b8 = a8 + (nv << 3);
+  for (long long r = a + threadIdx.x; r < a8; r += ACC_THREADS)
+    acc_record<WEIGHTED>(c, s, e, rec_bin[r], WEIGHTED ? rec_w[r] : 0.f);
+  for (long long r = b8 + threadIdx.x; r < b; r += ACC_THREADS)
+    acc_record<WEIGHTED>(c, s, e, rec_bin[r], WEIGHTED ? rec_w[r] : 0.f);
+  const uint4* vb = reinterpret_cast<const uint4*>(rec_bin + a8);
+  const float4* vw = reinterpret_cast<const float4*>(WEIGHTED ? rec_w + a8 : nullptr);
+  long long v = threadIdx.x;
+  for (; v + ACC_THREADS < nv; v += 2 * ACC_THREADS) {
+    const uint4 q0 = __ldcs(vb + v), q1 = __ldcs(vb + v + ACC_THREADS);
+    float4 w0 = z4, w1 = z4, w2 = z4, w3 = z4;
+    if (WEIGHTED) {
+      w0 = __ldcs(vw + 2 * v);
+      w1 = __ldcs(vw + 2 * v + 1);
+      w2 = __ldcs(vw + 2 * (v + ACC_THREADS));
+      w3 = __ldcs(vw + 2 * (v + ACC_THREADS) + 1);
+    }
+    acc_vec<WEIGHTED>(c, s, e, q0, w0, w1);
+    acc_vec<WEIGHTED>(c, s, e, q1, w2, w3);
+  }
+  if (v < nv) {
+    const uint4 q0 = __ldcs(vb + v);
+    float4 w0 = z4, w1 = z4;
+    if (WEIGHTED) {
+      w0 = __ldcs(vw + 2 * v);
+      w1 = __ldcs(vw + 2 * v + 1);
+    }
+    acc_vec<WEIGHTED>(c, s, e, q0, w0, w1);
+  }
+}
+
+template <bool WEIGHTED>
 __global__ void __launch_bounds__(ACC_THREADS)
-tile_accumulate_kernel(int ntiles, const long long* __restrict__ off, const long long* __restrict__ P,
+tile_accumulate_kernel(int nv, const long long* __restrict__ off, const long long* __restrict__ PV,
                        const unsigned short* __restrict__ rec_bin, const float* __restrict__ rec_w,
                        unsigned* __restrict__ pc, float* __restrict__ ps, float* __restrict__ pe) {
-  extern __shared__ __align__(16) unsigned char sm[];
+  extern __shared__ __align__(128) unsigned char sm[];
   unsigned* c = reinterpret_cast<unsigned*>(sm);
   float* s = reinterpret_cast<float*>(sm + TB * 4);
   float* e = reinterpret_cast<float*>(sm + TB * 8);
   const int G = gridDim.x, g = blockIdx.x;
-  const long long R = P[ntiles];
+  const long long R = PV[nv];
   const long long S1 = range_start(R, g + 1, G);
   long long pos = range_start(R, g, G);
-  int t = 0;
-  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  int v = 0;
   while (pos < S1) {
-    while (P[t + 1] <= pos) ++t;                 // pos < R = P[ntiles], so t < ntiles
-    const long long end = P[t + 1] < S1 ? P[t + 1] : S1;
+    while (PV[v + 1] <= pos) ++v;                // pos < R = PV[nv], so v < nv
+    const int t = v / NSUB;
+    const long long tend = PV[(t + 1) * NSUB] < S1 ? PV[(t + 1) * NSUB] : S1;
     for (int i = threadIdx.x; i < TB; i += ACC_THREADS) {
       c[i] = 0u;
       if (WEIGHTED) { s[i] = 0.f; e[i] = 0.f; }
     }
     __syncthreads();
-    // records [a, b) of the record arrays; bucket starts are multiples of 8
-    const long long a = off[t] + (pos - P[t]), b = off[t] + (end - P[t]);
-    long long a8 = (a + 7) & ~7ll;
-    if (a8 > b) a8 = b;
-    const long long nv = (b - a8) >> 3, b8 = a8 + (nv << 3);
-    for (long long r = a + threadIdx.x; r < a8; r += ACC_THREADS)
-      acc_record<WEIGHTED>(c, s, e, rec_bin[r], WEIGHTED ? rec_w[r] : 0.f);
-    for (long long r = b8 + threadIdx.x; r < b; r += ACC_THREADS)
-      acc_record<WEIGHTED>(c, s, e, rec_bin[r], WEIGHTED ? rec_w[r] : 0.f);
-    const uint4* vb = reinterpret_cast<const uint4*>(rec_bin + a8);
-    const float4* vw = reinterpret_cast<const float4*>(WEIGHTED ? rec_w + a8 : nullptr);
-    long long v = threadIdx.x;
-    for (; v + ACC_THREADS < nv; v += 2 * ACC_THREADS) {
-      const uint4 q0 = __ldcs(vb + v), q1 = __ldcs(vb + v + ACC_THREADS);
-      float4 w0 = z4, w1 = z4, w2 = z4, w3 = z4;
-      if (WEIGHTED) {
-        w0 = __ldcs(vw + 2 * v);
-        w1 = __ldcs(vw + 2 * v + 1);
-        w2 = __ldcs(vw + 2 * (v + ACC_THREADS));
-        w3 = __ldcs(vw + 2 * (v + ACC_THREADS) + 1);
-      }
-      acc_vec<WEIGHTED>(c, s, e, q0, w0, w1);
-      acc_vec<WEIGHTED>(c, s, e, q1, w2, w3);
-    }
-    if (v < nv) {
-      const uint4 q0 = __ldcs(vb + v);
-      float4 w0 = z4, w1 = z4;
-      if (WEIGHTED) {
-        w0 = __ldcs(vw + 2 * v);
-        w1 = __ldcs(vw + 2 * v + 1);
-      }
-      acc_vec<WEIGHTED>(c, s, e, q0, w0, w1);
+    // the sub-buckets of tile t inside [pos, tend)
+    while (pos < tend) {
+      while (PV[v + 1] <= pos) ++v;
+      const long long end = PV[v + 1] < tend ? PV[v + 1] : tend;
+      acc_range<WEIGHTED>(c, s, e, rec_bin, rec_w, off[v] + (pos - PV[v]), off[v] + (end - PV[v]));
+      pos = end;
     }
     __syncthreads();
     const long long slot = (long long)(g + t) * TB;
@@ -315,37 +463,37 @@ tile_accumulate_kernel(int ntiles, const long long* __restrict__ off, const long
       }
     }
     __syncthreads();
-    pos = end;
   }
 }
 
 // ---- pass 4: add the pieces of every bin's tile to the outputs ----------------------
 template <bool WEIGHTED>
 __global__ void __launch_bounds__(THREADS)
-tile_combine_kernel(long long nbins, int ntiles, int G, const long long* __restrict__ P,
+tile_combine_kernel(long long nbins, int nv, int G, const long long* __restrict__ PV,
                     const unsigned* __restrict__ pc, const float* __restrict__ ps, const float* __restrict__ pe,
                     const double* __restrict__ wacc, unsigned long long* __restrict__ counts,
                     float* __restrict__ wsum) {
-  const long long R = P[ntiles];
+  const long long R = PV[nv];
   for (long long bin = (long long)blockIdx.x * THREADS + threadIdx.x; bin < nbins;
        bin += (long long)gridDim.x * THREADS) {
     const int t = (int)(bin / TB);
     const long long i = bin - (long long)t * TB;
-    const long long lo = P[t], hi = P[t + 1];
+    const long long lo = PV[t * NSUB], hi = PV[(t + 1) * NSUB];
     unsigned long long cn = 0;
     double wv = 0.0;
     if (hi > lo) {
-      // the CTAs whose ranges meet [lo, hi), in order
+      // the CTAs whose ranges meet [lo, hi), in order: from the one holding lo
+      // to the one holding hi - 1 (every CTA range is non-empty when R >= G)
       int g = (int)(lo * G / R);
-      if (g > 0) --g;
-      for (; g < G; ++g) {
-        const long long s0 = range_start(R, g, G), s1 = range_start(R, g + 1, G);
-        if (s0 >= hi) break;
-        if ((s0 > lo ? s0 : lo) < (s1 < hi ? s1 : hi)) {
-          const long long slot = (long long)(g + t) * TB + i;
-          cn += pc[slot];
-          if (WEIGHTED) wv += (double)ps[slot] + (double)pe[slot];
-        }
+      while (g > 0 && range_start(R, g, G) > lo) --g;
+      while (g + 1 < G && range_start(R, g + 1, G) <= lo) ++g;
+      int gl = (int)((hi - 1) * G / R);
+      while (gl + 1 < G && range_start(R, gl + 1, G) <= hi - 1) ++gl;
+      for (; g <= gl; ++g) {
+        if (R < G && range_start(R, g, G) == range_start(R, g + 1, G)) continue;
+        const long long slot = (long long)(g + t) * TB + i;
+        cn += pc[slot];
+        if (WEIGHTED) wv += (double)ps[slot] + (double)pe[slot];
       }
     }
     counts[bin] += cn;
@@ -361,6 +509,17 @@ T* carve(char*& p, long long count) {
 }
 
 }  // namespace
+
+namespace nca {
+// NCA_OK or the error a histogram kernel recorded since the last read (cleared)
+int hist_read_status(cudaStream_t s) {
+  int v = 0, zero = 0;
+  check_cuda(cudaMemcpyFromSymbolAsync(&v, g_hist_status, sizeof(int), 0, cudaMemcpyDeviceToHost, s), "status read");
+  check_cuda(cudaMemcpyToSymbolAsync(g_hist_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s), "status clear");
+  check_cuda(cudaStreamSynchronize(s), "status sync");
+  return v;
+}
+}  // namespace nca
 
 extern "C" int32_t nca_hist2d(const float* x, const float* y, const float* w, int64_t n, int32_t nbx, int32_t nby,
                               double x_lo, double x_hi, double y_lo, double y_hi, uint64_t* counts, float* wsum,
@@ -390,7 +549,9 @@ extern "C" int32_t nca_hist2d(const float* x, const float* y, const float* w, in
     const long long ntiles = (nbins + TB - 1) / TB;
     const bool weighted = w != nullptr;
     unsigned long long* cnt = (unsigned long long*)counts;
-    if (ntiles > MAX_TILES || n < (1 << 20)) {
+    // the bulk copies of the partitioned path need 16-byte aligned point arrays
+    const bool aligned = ((uintptr_t)x % 16 == 0) && ((uintptr_t)y % 16 == 0) && (!weighted || (uintptr_t)w % 16 == 0);
+    if (ntiles > MAX_TILES || n < (1 << 20) || !aligned) {
       StreamScratch acc(weighted ? (size_t)nbins * sizeof(double) : 0, s);
       double* wacc = (double*)acc.ptr;
       if (weighted) check_cuda(cudaMemsetAsync(wacc, 0, (size_t)nbins * sizeof(double), s), "memset weights");
@@ -407,60 +568,78 @@ extern "C" int32_t nca_hist2d(const float* x, const float* y, const float* w, in
       }
       return;
     }
-    // persistent accumulate grid: as many CTAs as fit with the tile in shared memory
-    const size_t smem = weighted ? (size_t)TB * 12 : (size_t)TB * 4;
-    const void* acc_fn = weighted ? (const void*)tile_accumulate_kernel<true> : (const void*)tile_accumulate_kernel<false>;
-    check_cuda(cudaFuncSetAttribute(acc_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
-    int per_sm = 0;
-    check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, acc_fn, ACC_THREADS, smem), "occupancy");
-    if (per_sm < 1) per_sm = 1;
-    const int G = sms * per_sm;
-    // bucket storage bound: the sample has at most nsamp points, and the
-    // capacities add up to at most 1.25 * SAMPLE * nsamp + 4096 per tile
-    const long long nsamp = (((n + 1023) / 1024 + SAMPLE - 1) / SAMPLE) * 1024;
-    const long long maxrec = (long long)(SAMPLE * 5 / 4) * nsamp + 4096 * ntiles;
-    const long long nslots = (long long)(G + ntiles) * TB;
-    const size_t bytes = 5 * 256 + (size_t)(ntiles + 1) * 8 * 4 + (size_t)ntiles * 4 + (size_t)maxrec * 2 +
-                         (weighted ? (size_t)maxrec * 4 : 0) + (size_t)nslots * (weighted ? 12 : 4) + 8 * 256;
-    StreamScratch scratch(bytes, s);
-    StreamScratch acc(weighted ? (size_t)nbins * sizeof(double) : 0, s);
-    double* wacc = (double*)acc.ptr;
-    if (weighted) check_cuda(cudaMemsetAsync(wacc, 0, (size_t)nbins * sizeof(double), s), "memset weights");
-    char* p = (char*)(((uintptr_t)scratch.ptr + 255) & ~(uintptr_t)255);
-    long long* off = carve<long long>(p, ntiles + 1);
-    long long* cap = carve<long long>(p, ntiles + 1);
-    unsigned long long* fill = carve<unsigned long long>(p, ntiles + 1);
-    long long* P = carve<long long>(p, ntiles + 1);
-    unsigned* est = carve<unsigned>(p, ntiles);
-    float* rec_w = weighted ? carve<float>(p, maxrec) : nullptr;
-    unsigned short* rec_bin = carve<unsigned short>(p, maxrec);
-    unsigned* pc = carve<unsigned>(p, nslots);
-    float* ps = weighted ? carve<float>(p, nslots) : nullptr;
-    float* pe = weighted ? carve<float>(p, nslots) : nullptr;
-    check_cuda(cudaMemsetAsync(est, 0, ntiles * 4, s), "memset estimates");
-    tile_sample_kernel<<<(unsigned)std::min<long long>((nsamp + THREADS - 1) / THREADS, (long long)sms * 4), THREADS, 0,
-                         s>>>(x, y, n, B, (int)ntiles, est);
-    tile_plan_kernel<<<1, MAX_TILES, 0, s>>>(est, (int)ntiles, off, cap, fill);
-    const long long chunks = (n + CHUNK - 1) / CHUNK;
-    if (weighted)
-      tile_scatter_kernel<true><<<(unsigned)chunks, THREADS, 0, s>>>(x, y, w, n, B, (int)ntiles, off, cap, fill, rec_bin,
-                                                                     rec_w, cnt, wacc);
-    else
-      tile_scatter_kernel<false><<<(unsigned)chunks, THREADS, 0, s>>>(x, y, nullptr, n, B, (int)ntiles, off, cap, fill,
-                                                                      rec_bin, nullptr, cnt, nullptr);
-    tile_prefix_kernel<<<1, MAX_TILES, 0, s>>>((int)ntiles, cap, fill, P);
-    if (weighted)
-      tile_accumulate_kernel<true><<<G, ACC_THREADS, smem, s>>>((int)ntiles, off, P, rec_bin, rec_w, pc, ps, pe);
-    else
-      tile_accumulate_kernel<false><<<G, ACC_THREADS, smem, s>>>((int)ntiles, off, P, rec_bin, nullptr, pc, nullptr,
-                                                                 nullptr);
-    const unsigned cgrid = (unsigned)std::min<long long>((nbins + THREADS - 1) / THREADS, (long long)sms * 8);
-    if (weighted)
-      tile_combine_kernel<true><<<cgrid, THREADS, 0, s>>>(nbins, (int)ntiles, G, P, pc, ps, pe, wacc, cnt, wsum);
-    else
-      tile_combine_kernel<false><<<cgrid, THREADS, 0, s>>>(nbins, (int)ntiles, G, P, pc, nullptr, nullptr, nullptr,
-                                                           cnt, nullptr);
-    check_cuda(cudaGetLastError(), "hist2d launches");
-    count_launch(6);
+    // partitioned path, at most 2^30 points per pass so that record indices
+    // fit in 31 bits; longer inputs add up pass by pass
+    auto pass = [&](const float* x, const float* y, const float* w, long long n) {
+      // persistent accumulate grid: as many CTAs as fit with the tile in shared memory
+      const size_t smem = weighted ? (size_t)TB * 12 : (size_t)TB * 4;
+      const void* acc_fn = weighted ? (const void*)tile_accumulate_kernel<true> : (const void*)tile_accumulate_kernel<false>;
+      check_cuda(cudaFuncSetAttribute(acc_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attribute");
+      int per_sm = 0;
+      check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, acc_fn, ACC_THREADS, smem), "occupancy");
+      if (per_sm < 1) per_sm = 1;
+      const int G = sms * per_sm;
+      // bucket storage bound: the sample has at most nsamp points, so the
+      // capacities add up to at most 1.25 * SAMPLE * nsamp + (SLACK + 8) per bucket
+      const long long nv = ntiles * NSUB;
+      const long long nsamp = (((n + 1023) / 1024 + SAMPLE - 1) / SAMPLE) * 1024;
+      const long long maxrec = (long long)(SAMPLE * 5 / 4) * nsamp + (long long)(SLACK + 8) * nv;
+      const long long nslots = (long long)(G + ntiles) * TB;
+      const size_t bytes = 16 * 256 + (size_t)(nv + 1) * 8 * 3 + (size_t)nv * FPAD * 8 + (size_t)ntiles * EPAD * 4 +
+                           (size_t)maxrec * 2 + (weighted ? (size_t)maxrec * 4 : 0) + (size_t)nslots * (weighted ? 12 : 4);
+      StreamScratch scratch(bytes, s);
+      StreamScratch acc(weighted ? (size_t)nbins * sizeof(double) : 0, s);
+      double* wacc = (double*)acc.ptr;
+      if (weighted) check_cuda(cudaMemsetAsync(wacc, 0, (size_t)nbins * sizeof(double), s), "memset weights");
+      char* p = (char*)(((uintptr_t)scratch.ptr + 255) & ~(uintptr_t)255);
+      long long* off = carve<long long>(p, nv + 1);
+      long long* cap = carve<long long>(p, nv + 1);
+      long long* PV = carve<long long>(p, nv + 1);
+      unsigned long long* fill = carve<unsigned long long>(p, nv * FPAD);
+      unsigned* est = carve<unsigned>(p, ntiles * EPAD);
+      float* rec_w = weighted ? carve<float>(p, maxrec) : nullptr;
+      unsigned short* rec_bin = carve<unsigned short>(p, maxrec);
+      unsigned* pc = carve<unsigned>(p, nslots);
+      float* ps = weighted ? carve<float>(p, nslots) : nullptr;
+      float* pe = weighted ? carve<float>(p, nslots) : nullptr;
+      check_cuda(cudaMemsetAsync(est, 0, (size_t)ntiles * EPAD * 4, s), "memset estimates");
+      tile_sample_kernel<<<(unsigned)std::min<long long>((nsamp + THREADS - 1) / THREADS, (long long)sms * 4), THREADS, 0,
+                           s>>>(x, y, n, B, (int)ntiles, est);
+      tile_plan_kernel<<<1, SCAN_THREADS, 0, s>>>(est, (int)nv, off, cap, fill);
+      // persistent scatter grid: every resident CTA, at most one per chunk
+      {
+        const long long chunks = (n + CHUNK - 1) / CHUNK;
+        const int ssm = weighted ? scatter_smem<true>() : scatter_smem<false>();
+        const void* sc_fn = weighted ? (const void*)tile_scatter_kernel<true> : (const void*)tile_scatter_kernel<false>;
+        check_cuda(cudaFuncSetAttribute(sc_fn, cudaFuncAttributeMaxDynamicSharedMemorySize, ssm), "smem attribute");
+        int sper = 0;
+        check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&sper, sc_fn, THREADS, ssm), "occupancy");
+        const unsigned sgrid = (unsigned)std::min<long long>(chunks, (long long)sms * std::max(sper, 1));
+        if (weighted)
+          tile_scatter_kernel<true><<<sgrid, THREADS, ssm, s>>>(x, y, w, n, B, (int)ntiles, off, cap, fill, rec_bin, rec_w,
+                                                                cnt, wacc);
+        else
+          tile_scatter_kernel<false><<<sgrid, THREADS, ssm, s>>>(x, y, nullptr, n, B, (int)ntiles, off, cap, fill,
+                                                                 rec_bin, nullptr, cnt, nullptr);
+      }
+      tile_prefix_kernel<<<1, SCAN_THREADS, 0, s>>>((int)nv, cap, fill, PV);
+      if (weighted)
+        tile_accumulate_kernel<true><<<G, ACC_THREADS, smem, s>>>((int)nv, off, PV, rec_bin, rec_w, pc, ps, pe);
+      else
+        tile_accumulate_kernel<false><<<G, ACC_THREADS, smem, s>>>((int)nv, off, PV, rec_bin, nullptr, pc, nullptr,
+                                                                   nullptr);
+      const unsigned cgrid = (unsigned)std::min<long long>((nbins + THREADS - 1) / THREADS, (long long)sms * 8);
+      if (weighted)
+        tile_combine_kernel<true><<<cgrid, THREADS, 0, s>>>(nbins, (int)nv, G, PV, pc, ps, pe, wacc, cnt, wsum);
+      else
+        tile_combine_kernel<false><<<cgrid, THREADS, 0, s>>>(nbins, (int)nv, G, PV, pc, nullptr, nullptr, nullptr,
+                                                             cnt, nullptr);
+      check_cuda(cudaGetLastError(), "hist2d launches");
+      count_launch(6);
+    };
+    for (long long s0 = 0; s0 < n; s0 += (1ll << 30)) {
+      const long long len = std::min<long long>(n - s0, 1ll << 30);
+      pass(x + s0, y + s0, weighted ? w + s0 : nullptr, len);
+    }
   });
 }
