@@ -11,6 +11,7 @@ using namespace nca;
 namespace nca {
 int stencil_read_status(cudaStream_t s);
 int hist_read_status(cudaStream_t s);
+int jit_read_status(cudaStream_t s);
 }
 
 extern "C" {
@@ -26,7 +27,8 @@ int32_t nca_device_status(int32_t* status, void* stream) {
     if (!status) fail(NCA_ERR_INVALID, "null status");
     const int st = stencil_read_status((cudaStream_t)stream);
     const int hs = hist_read_status((cudaStream_t)stream);
-    *status = st != 0 ? st : hs;
+    const int js = jit_read_status((cudaStream_t)stream);
+    *status = st != 0 ? st : hs != 0 ? hs : js;
   });
 }
 

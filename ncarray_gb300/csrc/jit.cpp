@@ -295,11 +295,15 @@ struct Spec {
   int grp = 4;     // kind 6: loop indices whose loads are issued together
   uint32_t tmask = 0;
   int tile_bytes = 0;
+  // kind 7 (bulk-copy staged): stages, p-row / uniform operand masks, fastest
+  // loop dim, number of p-row operands, log2(tp / 8)
+  int ns = 0, ld = 0, npc = 0, ltp8 = 3, nmaps = 1;
+  uint32_t pmask = 0, umask = 0;
 };
 
 struct WordLayout {
   int opb, ops, outb, outs, shape, scal, redb, reds, total, psum, pmax, pmin, nsplit, chunk,
-      keptn, redn, magic, nwords;
+      keptn, redn, status, magic, nwords;
 };
 
 // symbol of each kernel class (distinct names keep profiler launch lists readable)
@@ -311,6 +315,8 @@ static const char* kernel_name(int kind) {
     case 4: return "nca_red_outer";
     case 5: return "nca_finalize";
     case 6: return "nca_staged";
+    case 7: return "nca_staged_async";
+    case 8: return "nca_staged_merge";
   }
   return "nca_kernel";
 }
@@ -327,7 +333,7 @@ static WordLayout word_layout(int nops, int nd, int nscal, int nred) {
   L.redb = p; p += nred;
   L.reds = p; p += nred * nd;
   L.total = p++; L.psum = p++; L.pmax = p++; L.pmin = p++; L.nsplit = p++; L.chunk = p++;
-  L.keptn = p++; L.redn = p++;
+  L.keptn = p++; L.redn = p++; L.status = p++;
   L.magic = p; p += nd;
   L.nwords = p;
   return L;
@@ -497,7 +503,11 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_W_REDB " << L.redb << "\n#define NCA_W_REDS " << L.reds << "\n#define NCA_W_TOTAL " << L.total
      << "\n#define NCA_W_PSUM " << L.psum << "\n#define NCA_W_PMAX " << L.pmax << "\n#define NCA_W_PMIN " << L.pmin
      << "\n#define NCA_W_NSPLIT " << L.nsplit << "\n#define NCA_W_CHUNK " << L.chunk << "\n#define NCA_W_KEPTN " << L.keptn
-     << "\n#define NCA_W_REDN " << L.redn << "\n#define NCA_W_MAGIC " << L.magic << "\n";
+     << "\n#define NCA_W_REDN " << L.redn << "\n#define NCA_W_STATUS " << L.status << "\n#define NCA_W_MAGIC " << L.magic
+     << "\n";
+  os << "#define NCA_NS " << sp.ns << "\n#define NCA_LD " << sp.ld << "\n#define NCA_NPC " << sp.npc << "\n#define NCA_LTP8 "
+     << sp.ltp8 << "\n#define NCA_PMASK " << sp.pmask << "u\n#define NCA_UMASK " << sp.umask << "u\n#define NCA_NMAPS "
+     << sp.nmaps << "\n";
   os << "typedef " << dtinfo(sp.w).ctype << " nca_w;\n";
   const std::string rty = sp.nred > 0 ? cty(sp.r) : std::string("nca_w");
   os << "typedef " << rty << " nca_r;\n";
@@ -812,6 +822,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.kept_mask); add(sp.has_out); add(sp.out_dtype); add(sp.w); add(sp.r); add(sp.nred); add(sp.red_ops);
   add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
+  add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps);
   for (int d : sp.op_dtypes) add(d);
   k += '|';
   for (int m : sp.op_modes) add(m);
@@ -833,7 +844,7 @@ static CUfunction kernel_for(const Spec& sp, const Tape& t) {
     if (it != cache.end()) return it->second;
   }
   CUfunction fn = jit_get(gen_source(sp, t), kernel_name(sp.kind));
-  if (sp.kind == 6) {
+  if (sp.kind == 6 || sp.kind == 7) {
     // the staged class lives on shared memory: ask for the largest carveout
     check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100), "carveout");
   }
@@ -885,6 +896,20 @@ static void plan_vec(const Space& s, Spec& sp, int max_vec_elems, bool with_out)
   }
 }
 
+// The device int that JIT kernels set when a bounded wait gives up (a
+// __device__ variable of this library, so no allocation is ever needed).
+int* jit_status_word();
+
+// reads and clears the JIT status word of the current device (synchronises s)
+int jit_read_status(cudaStream_t s) {
+  int* p = jit_status_word();
+  int v = 0;
+  check_cuda(cudaMemcpyAsync(&v, p, sizeof(int), cudaMemcpyDeviceToHost, s), "status read");
+  check_cuda(cudaMemsetAsync(p, 0, sizeof(int), s), "status clear");
+  check_cuda(cudaStreamSynchronize(s), "status sync");
+  return v ? NCA_ERR_TIMEOUT : 0;
+}
+
 static void fill_common_words(const Space& s, const Spec& sp, const Tape& t, const WordLayout& L,
                               std::vector<uint64_t>& w) {
   w.assign(L.nwords, 0);
@@ -903,6 +928,7 @@ static void fill_common_words(const Space& s, const Spec& sp, const Tape& t, con
     for (int d = 0; d < sp.nd; ++d) w[L.reds + k * sp.nd + d] = (uint64_t)s.reds[k].st[d];
   }
   w[L.total] = (uint64_t)s.total();
+  w[L.status] = (uint64_t)(uintptr_t)jit_status_word();
 }
 
 static void launch(CUfunction fn, int64_t grid, std::vector<uint64_t>& words, cudaStream_t stream,
@@ -968,10 +994,160 @@ static int find_staged(const Space& s, uint32_t& tmask, int& nt) {
   return qd;
 }
 
+// Kind 7: the staged shape with 4-byte elements whose tiles TMA can move (see
+// the template). Returns false, launching nothing, when the views do not
+// allow it.
+static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int qd, uint32_t tmask, int nt, int64_t KN,
+                                int64_t RN, cudaStream_t stream) {
+  // NCA_STAGED_ASYNC=0 keeps these views on kind 6 (read on every call)
+  if (const char* e = getenv("NCA_STAGED_ASYNC")) if (e[0] == '0') return false;
+  if (!drv().cuTensorMapEncodeTiled) return false;
+  const int pd = s.nd - 1;
+  const int64_t P = s.shape[pd], QX = s.shape[qd];
+  if (s.nd < 3 || s.nd > 5) return false;
+  if (!(QX == 4 || QX == 8 || QX == 16 || QX == 32) || P % 32 != 0 || RN <= 0) return false;
+  if (KN >= (1ll << 31) || RN >= (1ll << 31)) return false;
+  if (sp.has_out && (dtinfo(s.out.dtype).size != 4 || s.out.st[pd] != 4)) return false;
+  for (int k = 0; k < sp.nops; ++k) if (dtinfo(s.ops[k].dtype).size != 4) return false;
+  int ld = -1;   // the fastest loop dim
+  for (int d = pd - 1; d >= 0; --d) if (s.red[d]) { ld = d; break; }
+  if (ld < 0 || ld == qd) return false;
+  const int64_t LX = s.shape[ld];
+  if (QX * LX >= (1ll << 31)) return false;
+  auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+  auto st_ok = [](int64_t st) { return st > 0 && st % 16 == 0 && st < (1ll << 40); };
+  // every dim but p (and q, ld when listed) has a positive 16-byte multiple stride
+  auto tma_ok = [&](const CArr& a, bool staged) {
+    if (!al16(a.base)) return false;
+    for (int d = 0; d <= pd; ++d) {
+      if (d == pd) { if (staged ? !st_ok(a.st[d]) : a.st[d] != 4) return false; continue; }
+      if (staged && d == qd) { if (a.st[d] != 4) return false; continue; }
+      if (staged && d == ld) { if (a.st[d] != QX * 4) return false; continue; }
+      if (!st_ok(a.st[d])) return false;
+    }
+    return true;
+  };
+  uint32_t pmask = 0, umask = 0;
+  int npc = 0;
+  for (int k = 0; k < sp.nops; ++k) {
+    const CArr& a = s.ops[k];
+    if ((tmask >> k) & 1u) {
+      if (!tma_ok(a, true)) return false;
+    } else if (a.st[pd] == 4) {
+      if (!tma_ok(a, false)) return false;
+      pmask |= 1u << k;
+      ++npc;
+    } else if (a.st[pd] == 0) {
+      if (a.st[qd] == 0 && a.st[ld] == 0) umask |= 1u << k;
+    } else {
+      return false;
+    }
+  }
+  if (sp.has_out && !tma_ok(s.out, false)) return false;
+  // block of rb loop indices: a divisor of the fastest loop extent whose
+  // (loop index, q) rows fill whole 128-byte boxes, at most 128 of them
+  int rb = 0;
+  for (int c = 16; c >= 1; c /= 2)
+    if (LX % c == 0 && c * QX <= 128 && (c * QX) % 32 == 0) { rb = c; break; }
+  if (rb == 0) return false;
+  const int tp = 32, rowq = rb * (int)QX;
+  const int64_t xt = (int64_t)(rowq / 32) * tp * 128, kt = (int64_t)rowq * 128;
+  const int64_t stage = nt * xt + npc * kt;
+  int ns = 4;
+  auto smem_of = [&](int n) { return n * stage + 2 * kt + 8 * n + 1024; };
+  while (ns > 2 && smem_of(ns) > 200 * 1024) --ns;
+  if (smem_of(ns) > 200 * 1024) return false;
+  const unsigned smem = (unsigned)smem_of(ns);
+  sp.kind = 7;
+  sp.nd = s.nd;
+  sp.vec = 1;
+  sp.op_modes.assign(sp.nops, M_CONST);
+  for (int k = 0; k < sp.nops; ++k) {
+    if ((tmask >> k) & 1u) sp.op_modes[k] = M_STAGED;
+    else if ((pmask >> k) & 1u) sp.op_modes[k] = M_CONTIG;
+  }
+  sp.kept_mask = 0;
+  for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
+  int qxp = 1;
+  while (qxp < QX) qxp *= 2;
+  sp.qd = qd; sp.qx = (int)QX; sp.qxp = qxp; sp.tp = tp; sp.rb = rb; sp.tmask = tmask; sp.tile_bytes = 0;
+  sp.ns = ns; sp.ld = ld; sp.npc = npc; sp.pmask = pmask; sp.umask = umask; sp.ltp8 = 2;
+  sp.nmaps = nt + npc + (sp.has_out ? 1 : 0);
+  sp.minb = 1; sp.grp = 1;
+  // tensor maps: staged operands, p operands, the stored value
+  struct alignas(64) Maps { CUtensorMap m[NCA_MAX_OPERANDS + 1]; };
+  Maps maps;
+  memset(&maps, 0, sizeof(maps));
+  std::vector<int> other;
+  for (int d = 0; d < pd; ++d) if (d != qd && d != ld) other.push_back(d);
+  auto encode = [&](CUtensorMap* m, const CArr& a, bool staged) {
+    cuuint64_t dims[5], strides[4];
+    cuuint32_t box[5], estr[5] = {1u, 1u, 1u, 1u, 1u};
+    int r = 0;
+    if (staged) {
+      dims[0] = (cuuint64_t)(QX * LX); box[0] = 32;
+      dims[1] = (cuuint64_t)P; strides[0] = (cuuint64_t)a.st[pd]; box[1] = (cuuint32_t)tp;
+      r = 2;
+    } else {
+      dims[0] = (cuuint64_t)P; box[0] = (cuuint32_t)tp;
+      dims[1] = (cuuint64_t)QX; strides[0] = (cuuint64_t)a.st[qd]; box[1] = (cuuint32_t)QX;
+      dims[2] = (cuuint64_t)LX; strides[1] = (cuuint64_t)a.st[ld]; box[2] = (cuuint32_t)rb;
+      r = 3;
+    }
+    for (int d : other) { dims[r] = (cuuint64_t)s.shape[d]; strides[r - 1] = (cuuint64_t)a.st[d]; box[r] = 1; ++r; }
+    check_cu(drv().cuTensorMapEncodeTiled(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, (cuuint32_t)r, const_cast<char*>(a.base),
+                                          dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE),
+             "cuTensorMapEncodeTiled");
+  };
+  int mi = 0;
+  for (int k = 0; k < sp.nops; ++k) if ((tmask >> k) & 1u) encode(&maps.m[mi++], s.ops[k], true);
+  for (int k = 0; k < sp.nops; ++k) if ((pmask >> k) & 1u) encode(&maps.m[mi++], s.ops[k], false);
+  if (sp.has_out) encode(&maps.m[mi++], s.out, false);
+  CUfunction fn = kernel_for(sp, tape);
+  const int sms = sm_count(current_device());
+  int per_sm = 0;
+  check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem), "smem attribute");
+  check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem), "occupancy");
+  if (per_sm < 1) return false;
+  const int64_t U = KN / ((int64_t)tp * QX), NB = RN / rb, W = U * NB;
+  const int64_t G = std::min<int64_t>((int64_t)sms * per_sm, W);
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  std::vector<uint64_t> w;
+  fill_common_words(s, sp, tape, L, w);
+  w[L.nsplit] = (uint64_t)G; w[L.chunk] = 0; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+  const int64_t slots = (G + U) * (int64_t)tp * QX;
+  StreamScratch part(sp.nred > 0 ? (size_t)slots * 8 * ((sp.has_sum ? 1 : 0) + (sp.has_max ? 2 : 0) + (sp.has_min ? 2 : 0)) : 0,
+                     stream);
+  if (sp.nred > 0) {
+    uint64_t* p = (uint64_t*)part.ptr;
+    if (sp.has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += slots; }
+    if (sp.has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * slots; }
+    if (sp.has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * slots; }
+  }
+  // the kernel takes the words and the first nmaps tensor maps
+  std::vector<unsigned char> mp(sizeof(CUtensorMap) * sp.nmaps + 64);
+  unsigned char* mpa = (unsigned char*)(((uintptr_t)mp.data() + 63) & ~(uintptr_t)63);
+  memcpy(mpa, &maps, sizeof(CUtensorMap) * sp.nmaps);
+  void* params[] = {w.data(), mpa};
+  count_launch();
+  check_cu(drv().cuLaunchKernel(fn, (unsigned)G, 1, 1, 256, 1, 1, smem, (CUstream)stream, params, nullptr),
+           "cuLaunchKernel");
+  if (sp.nred > 0) {
+    Spec fs = sp;
+    fs.kind = 8;
+    CUfunction ff = kernel_for(fs, tape);
+    launch(ff, std::min<int64_t>(cdiv(U * tp * QX, 256), (int64_t)sms * 8), w, stream);
+  }
+  return true;
+}
+
 // Launches kind 6 (and its finalize when the loop dims are split). Kept dims
 // are those with s.red false; KN / RN are the kept / loop element counts.
 static void launch_staged(const Space& s, Spec sp, const Tape& tape, int qd, uint32_t tmask, int nt, int64_t KN,
                           int64_t RN, cudaStream_t stream) {
+  if (launch_staged_async(s, sp, tape, qd, tmask, nt, KN, RN, stream)) return;
   const int sms = sm_count(current_device());
   const int pd = s.nd - 1;
   const int64_t P = s.shape[pd], QX = s.shape[qd];
@@ -1355,6 +1531,29 @@ int jit_selftest(const char* arch) {
     sp.nred = 0; sp.red_ops = 0; sp.has_max = false; sp.kept_mask = 1u | 8u;
     nvrtc_compile(gen_source(sp, t), a);
     ++n;
+    // kinds 7 and 8 (4-byte operands and result): operand 0 staged, 1 in p rows, 2 uniform
+    if (dtinfo(d[2]).size == 4 && dtinfo(d[1]).size == 4) {
+      Spec a7;
+      a7.kind = 7; a7.nops = 3; a7.nd = 4; a7.vec = 1; a7.w = d[0]; a7.r = d[1]; a7.out_dtype = d[1]; a7.nscal = 1;
+      a7.op_dtypes = {d[2], d[2], d[2]};
+      a7.op_modes = {M_STAGED, M_CONTIG, M_CONST};
+      a7.has_out = true; a7.nred = 2; a7.red_ops = 2u | (4u << 4); a7.has_max = true;
+      a7.kept_mask = 1u | 2u | 8u; a7.qd = 0; a7.qx = 8; a7.qxp = 8; a7.tp = 32; a7.ltp8 = 2; a7.rb = 16;
+      a7.tmask = 1u; a7.pmask = 2u; a7.umask = 4u; a7.npc = 1; a7.ns = 4; a7.ld = 2; a7.nmaps = 3;
+      nvrtc_compile(gen_source(a7, t), a);
+      ++n;
+      Spec a8 = a7;
+      a8.kind = 8;
+      nvrtc_compile(gen_source(a8, t), a);
+      ++n;
+      a7.nred = 0; a7.red_ops = 0; a7.has_max = false; a7.kept_mask = 1u | 8u;
+      nvrtc_compile(gen_source(a7, t), a);
+      // five dims: two other dims besides p, q and the fastest loop dim
+      a7.nd = 5; a7.kept_mask = 1u | 2u | 16u; a7.ld = 3; a7.nred = 2; a7.red_ops = 2u | (4u << 4); a7.has_max = true;
+      nvrtc_compile(gen_source(a7, t), a);
+      ++n;
+      ++n;
+    }
   }
   return n;
 }

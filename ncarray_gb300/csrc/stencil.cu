@@ -20,6 +20,8 @@
 #include <cstdint>
 #include <cstring>
 
+#include <mutex>
+
 #include "common.hpp"
 
 namespace {
@@ -28,6 +30,7 @@ constexpr int TX = 64, TY = 16, NST = 4, THREADS = 256;
 constexpr unsigned long long kWaitNs = 2000000000ull;
 
 static __device__ int g_stencil_status;
+__device__ int g_jit_status;   // set by JIT kernels (kind 7) whose bounded waits give up
 
 template <class T>
 struct Weights {
@@ -344,6 +347,21 @@ void run(const nca_view* a, const nca_view* b, const double* w27, double dt, int
 }  // namespace
 
 namespace nca {
+// address of the status word of JIT kernels on the current device
+int* jit_status_word() {
+  static std::mutex mu;
+  static int* addr[64] = {nullptr};
+  const int dev = current_device();
+  if (dev < 0 || dev >= 64) fail(NCA_ERR_LIMIT, "device %d", dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    check_cuda(cudaGetSymbolAddress(&p, g_jit_status), "status word address");
+    addr[dev] = static_cast<int*>(p);
+  }
+  return addr[dev];
+}
+
 // reads and clears the stencil status word (synchronises the stream)
 int stencil_read_status(cudaStream_t s) {
   int v = 0, zero = 0;

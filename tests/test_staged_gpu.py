@@ -1,8 +1,11 @@
 """Fused expressions + reductions whose operands are transposed relative to the
-output (staged through shared memory by the JIT kernel class 6), vs the oracle.
+output, staged through shared memory by the JIT kernel classes 6 (register
+staging, any layout) and 7 (bulk-copy staging of contiguous aligned rows, with
+the ordered merge of class 8), vs the oracle.
 
 Covers partial p tiles, q extents from 2 to 32, two staged operands, float64
-and int32 staged operands, several reduced axes and every reduction op.
+and int32 staged operands, several reduced axes, every reduction op, units
+split between CTAs, and each class-7 case again on class 6.
 Expression values bit-exact; reductions per tests/test_reduce_gpu.py."""
 import numpy as np
 import pytest
@@ -68,5 +71,58 @@ def test_staged_without_store(cuda, orc):
         y = dev(x).permute(3, 1, 2, 0) + 1.0
     mx, am = y.evaluate(reductions=[(RedOp.MAX, 2), (RedOp.ARGMAX, 2)])
     yr = oracle_eval(orc, y, [xp])
+    check_reduction(orc, yr, DType.float32, RedOp.MAX, 2, mx.to_host())
+    check_reduction(orc, yr, DType.float32, RedOp.ARGMAX, 2, am.to_host())
+
+
+# views that class 7 takes: 4-byte elements, p extent a multiple of 32,
+# q extent 4..32, rows 16-byte aligned
+ASYNC_CASES = [
+    ((8, 16, 32, 64), 2),        # the C2 layout family
+    ((8, 4, 2048, 64), 2),       # few units, each split between many CTAs
+    ((16, 6, 40, 96), (1, 2)),   # q = 16, p tiles of 32, two loop dims
+    ((32, 3, 16, 64), 2),        # q = 32: eight items per thread
+    ((4, 10, 64, 64), 2),        # q = 4
+]
+
+
+@pytest.mark.parametrize("async_on", ["1", "0"])
+@pytest.mark.parametrize("shape,axes", ASYNC_CASES)
+@pytest.mark.parametrize("op", [RedOp.MAX, RedOp.ARGMAX, RedOp.SUM, RedOp.MEAN, RedOp.MIN])
+def test_async_staged_reduce(cuda, orc, monkeypatch, async_on, shape, axes, op):
+    """C2's expression (staged x times a broadcast vector plus an int32 array
+    in p rows) on class 7, and the same views on class 6."""
+    monkeypatch.setenv("NCA_STAGED_ASYNC", async_on)
+    rng = np.random.default_rng(SEED + 73)
+    q, b, r, p = shape
+    x = rng.normal(size=(p, b, r, q)).astype(np.float32)
+    xp = x.transpose(3, 1, 2, 0)
+    vv = rng.normal(size=b).astype(np.float32)
+    k = rng.integers(-1000, 1001, xp.shape).astype(np.int32)
+    dx, dv, dk = dev(x).permute(3, 1, 2, 0), dev(vv).reshape(1, b, 1, 1), dev(k)
+    with nca.lazy_mode():
+        y = dx * dv + dk
+    out = nca.NCDevArray(y.shape, y.dtype)
+    (res,) = y.evaluate(out=out, reductions=[(op, axes)])
+    yr = oracle_eval(orc, y, [xp, vv.reshape(1, b, 1, 1), k])
+    assert_bits_equal(out.to_host(), yr, "stored value")
+    check_reduction(orc, yr, DType.float32, op, axes, res.to_host())
+
+
+@pytest.mark.parametrize("async_on", ["1", "0"])
+def test_async_staged_plain_and_argmax_ties(cuda, orc, monkeypatch, async_on):
+    """A transposed expression without reductions (one unit over all CTAs),
+    then max/argmax over values with many ties (first index must win)."""
+    monkeypatch.setenv("NCA_STAGED_ASYNC", async_on)
+    rng = np.random.default_rng(SEED + 74)
+    x = rng.integers(-3, 4, size=(64, 8, 512, 8)).astype(np.float32)
+    xp = x.transpose(3, 1, 2, 0)
+    with nca.lazy_mode():
+        y = dev(x).permute(3, 1, 2, 0) * 3.0 - 1.0
+    out = nca.NCDevArray(y.shape, y.dtype)
+    y.evaluate(out=out)
+    yr = oracle_eval(orc, y, [xp])
+    assert_bits_equal(out.to_host(), yr, "stored value")
+    mx, am = y.evaluate(reductions=[(RedOp.MAX, 2), (RedOp.ARGMAX, 2)])
     check_reduction(orc, yr, DType.float32, RedOp.MAX, 2, mx.to_host())
     check_reduction(orc, yr, DType.float32, RedOp.ARGMAX, 2, am.to_host())
