@@ -668,7 +668,7 @@ def main():
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": round(fused_gbs, 2), "peak": peak, "unit": "GB/s",
                      "frac": round(fused_gbs / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "fused expression + axis-2 max/argmax (JIT RED_OUTER)",
+                     "kernel": "nca_staged_async: TMA-staged fused expression + axis-2 max/argmax",
                      "bytes_per_launch": by["fused"], "ms_per_launch": round(ms_fused, 5)},
         "per_op": per_op,
         "gpu_launches": int(launches),

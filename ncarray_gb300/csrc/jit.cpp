@@ -298,12 +298,12 @@ struct Spec {
   // kind 7 (bulk-copy staged): stages, p-row / uniform operand masks, fastest
   // loop dim, number of p-row operands, log2(tp / 8)
   int ns = 0, ld = 0, npc = 0, ltp8 = 3, nmaps = 1;
-  uint32_t pmask = 0, umask = 0;
+  uint32_t pmask = 0, umask = 0, uumask = 0;
 };
 
 struct WordLayout {
   int opb, ops, outb, outs, shape, scal, redb, reds, total, psum, pmax, pmin, nsplit, chunk,
-      keptn, redn, status, magic, nwords;
+      keptn, redn, status, aux, magic, nwords;
 };
 
 // symbol of each kernel class (distinct names keep profiler launch lists readable)
@@ -316,7 +316,6 @@ static const char* kernel_name(int kind) {
     case 5: return "nca_finalize";
     case 6: return "nca_staged";
     case 7: return "nca_staged_async";
-    case 8: return "nca_staged_merge";
   }
   return "nca_kernel";
 }
@@ -333,7 +332,7 @@ static WordLayout word_layout(int nops, int nd, int nscal, int nred) {
   L.redb = p; p += nred;
   L.reds = p; p += nred * nd;
   L.total = p++; L.psum = p++; L.pmax = p++; L.pmin = p++; L.nsplit = p++; L.chunk = p++;
-  L.keptn = p++; L.redn = p++; L.status = p++;
+  L.keptn = p++; L.redn = p++; L.status = p++; L.aux = p++;
   L.magic = p; p += nd;
   L.nwords = p;
   return L;
@@ -503,10 +502,11 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_W_REDB " << L.redb << "\n#define NCA_W_REDS " << L.reds << "\n#define NCA_W_TOTAL " << L.total
      << "\n#define NCA_W_PSUM " << L.psum << "\n#define NCA_W_PMAX " << L.pmax << "\n#define NCA_W_PMIN " << L.pmin
      << "\n#define NCA_W_NSPLIT " << L.nsplit << "\n#define NCA_W_CHUNK " << L.chunk << "\n#define NCA_W_KEPTN " << L.keptn
-     << "\n#define NCA_W_REDN " << L.redn << "\n#define NCA_W_STATUS " << L.status << "\n#define NCA_W_MAGIC " << L.magic
+     << "\n#define NCA_W_REDN " << L.redn << "\n#define NCA_W_STATUS " << L.status << "\n#define NCA_W_AUX " << L.aux
+     << "\n#define NCA_W_MAGIC " << L.magic
      << "\n";
   os << "#define NCA_NS " << sp.ns << "\n#define NCA_LD " << sp.ld << "\n#define NCA_NPC " << sp.npc << "\n#define NCA_LTP8 "
-     << sp.ltp8 << "\n#define NCA_PMASK " << sp.pmask << "u\n#define NCA_UMASK " << sp.umask << "u\n#define NCA_NMAPS "
+     << sp.ltp8 << "\n#define NCA_PMASK " << sp.pmask << "u\n#define NCA_UMASK " << sp.umask << "u\n#define NCA_UUMASK " << sp.uumask << "u\n#define NCA_NMAPS "
      << sp.nmaps << "\n";
   os << "typedef " << dtinfo(sp.w).ctype << " nca_w;\n";
   const std::string rty = sp.nred > 0 ? cty(sp.r) : std::string("nca_w");
@@ -822,7 +822,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.kept_mask); add(sp.has_out); add(sp.out_dtype); add(sp.w); add(sp.r); add(sp.nred); add(sp.red_ops);
   add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
-  add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps);
+  add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask);
   for (int d : sp.op_dtypes) add(d);
   k += '|';
   for (int m : sp.op_modes) add(m);
@@ -1027,7 +1027,7 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
     }
     return true;
   };
-  uint32_t pmask = 0, umask = 0;
+  uint32_t pmask = 0, umask = 0, uumask = 0;
   int npc = 0;
   for (int k = 0; k < sp.nops; ++k) {
     const CArr& a = s.ops[k];
@@ -1038,7 +1038,12 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
       pmask |= 1u << k;
       ++npc;
     } else if (a.st[pd] == 0) {
-      if (a.st[qd] == 0 && a.st[ld] == 0) umask |= 1u << k;
+      if (a.st[qd] == 0 && a.st[ld] == 0) {
+        umask |= 1u << k;
+        bool unit_const = true;   // constant along every loop dim too
+        for (int d = 0; d < pd; ++d) if (s.red[d] && a.st[d] != 0) unit_const = false;
+        if (unit_const) uumask |= 1u << k;
+      }
     } else {
       return false;
     }
@@ -1046,17 +1051,23 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   if (sp.has_out && !tma_ok(s.out, false)) return false;
   // block of rb loop indices: a divisor of the fastest loop extent whose
   // (loop index, q) rows fill whole 128-byte boxes, at most 128 of them
-  int rb = 0;
+  // 64 (loop index, q) rows per block and 3 stages measured best on the C2
+  // views (about 65 KiB per CTA, so three CTAs share an SM)
+  int rb = 0, rb_max = (int)std::max<int64_t>(1, 64 / QX);
+  if (const char* e = getenv("NCA_STAGED_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) rb_max = v; }
   for (int c = 16; c >= 1; c /= 2)
-    if (LX % c == 0 && c * QX <= 128 && (c * QX) % 32 == 0) { rb = c; break; }
+    if (c <= rb_max && LX % c == 0 && c * QX <= 128 && (c * QX) % 32 == 0) { rb = c; break; }
   if (rb == 0) return false;
   const int tp = 32, rowq = rb * (int)QX;
   const int64_t xt = (int64_t)(rowq / 32) * tp * 128, kt = (int64_t)rowq * 128;
   const int64_t stage = nt * xt + npc * kt;
-  int ns = 4;
+  // as many stages (2..6) as fit in the 227 KiB a CTA may use
+  const int64_t budget = 227 * 1024;
+  int ns = 3;
   auto smem_of = [&](int n) { return n * stage + 2 * kt + 8 * n + 1024; };
-  while (ns > 2 && smem_of(ns) > 200 * 1024) --ns;
-  if (smem_of(ns) > 200 * 1024) return false;
+  if (const char* e = getenv("NCA_STAGED_STAGES")) { const int v = atoi(e); if (v >= 2 && v <= 6) ns = v; }
+  while (ns > 2 && smem_of(ns) > budget) --ns;
+  if (smem_of(ns) > budget) return false;
   const unsigned smem = (unsigned)smem_of(ns);
   sp.kind = 7;
   sp.nd = s.nd;
@@ -1071,11 +1082,11 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   int qxp = 1;
   while (qxp < QX) qxp *= 2;
   sp.qd = qd; sp.qx = (int)QX; sp.qxp = qxp; sp.tp = tp; sp.rb = rb; sp.tmask = tmask; sp.tile_bytes = 0;
-  sp.ns = ns; sp.ld = ld; sp.npc = npc; sp.pmask = pmask; sp.umask = umask; sp.ltp8 = 2;
+  sp.ns = ns; sp.ld = ld; sp.npc = npc; sp.pmask = pmask; sp.umask = umask; sp.uumask = uumask; sp.ltp8 = 2;
   sp.nmaps = nt + npc + (sp.has_out ? 1 : 0);
   sp.minb = 1; sp.grp = 1;
   // tensor maps: staged operands, p operands, the stored value
-  struct alignas(64) Maps { CUtensorMap m[NCA_MAX_OPERANDS + 1]; };
+  struct Maps { CUtensorMap m[NCA_MAX_OPERANDS + 1]; };
   Maps maps;
   memset(&maps, 0, sizeof(maps));
   std::vector<int> other;
@@ -1097,7 +1108,10 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
     for (int d : other) { dims[r] = (cuuint64_t)s.shape[d]; strides[r - 1] = (cuuint64_t)a.st[d]; box[r] = 1; ++r; }
     check_cu(drv().cuTensorMapEncodeTiled(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, (cuuint32_t)r, const_cast<char*>(a.base),
                                           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                          CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                          CU_TENSOR_MAP_SWIZZLE_128B,
+                                          // staged rows are read 4 boxes (512 bytes) at a time; p rows
+                                          // are 128-byte boxes whose neighbour belongs to another unit
+                                          staged ? CU_TENSOR_MAP_L2_PROMOTION_L2_256B : CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE),
              "cuTensorMapEncodeTiled");
   };
@@ -1117,14 +1131,19 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   std::vector<uint64_t> w;
   fill_common_words(s, sp, tape, L, w);
   w[L.nsplit] = (uint64_t)G; w[L.chunk] = 0; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+  // partial pieces of split units, and one arrival counter per unit (zeroed
+  // here; the merging CTA resets its unit's counter)
   const int64_t slots = (G + U) * (int64_t)tp * QX;
-  StreamScratch part(sp.nred > 0 ? (size_t)slots * 8 * ((sp.has_sum ? 1 : 0) + (sp.has_max ? 2 : 0) + (sp.has_min ? 2 : 0)) : 0,
-                     stream);
+  const size_t pbytes = sp.nred > 0 ? (size_t)slots * 8 * ((sp.has_sum ? 1 : 0) + (sp.has_max ? 2 : 0) + (sp.has_min ? 2 : 0)) : 0;
+  const size_t cbytes = sp.nred > 0 ? ((size_t)U * 4 + 255) / 256 * 256 : 0;
+  StreamScratch part(pbytes + cbytes, stream);
   if (sp.nred > 0) {
     uint64_t* p = (uint64_t*)part.ptr;
     if (sp.has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += slots; }
     if (sp.has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * slots; }
     if (sp.has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * slots; }
+    w[L.aux] = (uint64_t)(uintptr_t)p;
+    check_cuda(cudaMemsetAsync(p, 0, cbytes, stream), "unit counters");
   }
   // the kernel takes the words and the first nmaps tensor maps
   std::vector<unsigned char> mp(sizeof(CUtensorMap) * sp.nmaps + 64);
@@ -1134,12 +1153,6 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   count_launch();
   check_cu(drv().cuLaunchKernel(fn, (unsigned)G, 1, 1, 256, 1, 1, smem, (CUstream)stream, params, nullptr),
            "cuLaunchKernel");
-  if (sp.nred > 0) {
-    Spec fs = sp;
-    fs.kind = 8;
-    CUfunction ff = kernel_for(fs, tape);
-    launch(ff, std::min<int64_t>(cdiv(U * tp * QX, 256), (int64_t)sms * 8), w, stream);
-  }
   return true;
 }
 
@@ -1531,7 +1544,7 @@ int jit_selftest(const char* arch) {
     sp.nred = 0; sp.red_ops = 0; sp.has_max = false; sp.kept_mask = 1u | 8u;
     nvrtc_compile(gen_source(sp, t), a);
     ++n;
-    // kinds 7 and 8 (4-byte operands and result): operand 0 staged, 1 in p rows, 2 uniform
+    // kind 7 (4-byte operands and result): operand 0 staged, 1 in p rows, 2 uniform
     if (dtinfo(d[2]).size == 4 && dtinfo(d[1]).size == 4) {
       Spec a7;
       a7.kind = 7; a7.nops = 3; a7.nd = 4; a7.vec = 1; a7.w = d[0]; a7.r = d[1]; a7.out_dtype = d[1]; a7.nscal = 1;
@@ -1541,10 +1554,6 @@ int jit_selftest(const char* arch) {
       a7.kept_mask = 1u | 2u | 8u; a7.qd = 0; a7.qx = 8; a7.qxp = 8; a7.tp = 32; a7.ltp8 = 2; a7.rb = 16;
       a7.tmask = 1u; a7.pmask = 2u; a7.umask = 4u; a7.npc = 1; a7.ns = 4; a7.ld = 2; a7.nmaps = 3;
       nvrtc_compile(gen_source(a7, t), a);
-      ++n;
-      Spec a8 = a7;
-      a8.kind = 8;
-      nvrtc_compile(gen_source(a8, t), a);
       ++n;
       a7.nred = 0; a7.red_ops = 0; a7.has_max = false; a7.kept_mask = 1u | 8u;
       nvrtc_compile(gen_source(a7, t), a);
