@@ -356,13 +356,10 @@ def measure_c4(torch, nca, peak, reps=5):
     return out
 
 
-def measure_c5(torch, nca, peak, n_arrays=20000):
-    """C5: 20,000 1-D arrays, lengths log-uniform in [64, 2^22], half float32 and
-    half bfloat16, x = s * exp(N(0, 2)) with random signs; per array sum, mean,
-    max and sum(x*x - x): one persistent graph-replayed launch vs the plain
-    per-array per-op float64 launches."""
-    import oracle
-    from ncarray_gb300.batch import Batch
+def c5_arrays(torch, nca, n_arrays):
+    """n_arrays 1-D device arrays with lengths log-uniform in [64, 2^22],
+    alternately float32 and bfloat16, x = exp(N(0, 2)) with random signs,
+    generated on the device from a seed (views into two large buffers)."""
     rng = np.random.default_rng(SEED + 4)
     lens = np.round(np.exp(rng.uniform(np.log(64), np.log(2 ** 22), n_arrays))).astype(np.int64)
     is16 = np.arange(n_arrays) % 2 == 1
@@ -389,6 +386,17 @@ def measure_c5(torch, nca, peak, n_arrays=20000):
         else:
             arrays.append(nca.NCDevArray((L,), nca.DType.float32, _buf=b32, _offset=4 * o32))
             o32 += L
+    return rng, lens, arrays, tot32, tot16
+
+
+def measure_c5(torch, nca, peak, n_arrays=20000):
+    """C5: 20,000 1-D arrays, lengths log-uniform in [64, 2^22], half float32 and
+    half bfloat16, x = s * exp(N(0, 2)) with random signs; per array sum, mean,
+    max and sum(x*x - x): one persistent graph-replayed launch vs the plain
+    per-array per-op float64 launches."""
+    import oracle
+    from ncarray_gb300.batch import Batch
+    rng, lens, arrays, tot32, tot16 = c5_arrays(torch, nca, n_arrays)
     nbytes = 4 * tot32 + 2 * tot16
     B = Batch(arrays)
     sched = B.autotune()
@@ -457,6 +465,13 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
         counts = nca.NCDevArray((1024, 1024), nca.DType.uint64).fill(0)
         wsum = nca.NCDevArray((1024, 1024), nca.DType.float32).fill(0.0)
         fn = lambda: hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0), w, wsum)  # noqa: E731
+    elif op == "c5-small":
+        # the batched reduction on 1,000 of the uneven arrays (about 1 GB)
+        from ncarray_gb300.batch import Batch
+        _, _, arrays, _, _ = c5_arrays(torch, nca, 1000)
+        B = Batch(arrays)
+        B.run(graph=False)
+        fn = lambda: B.run(graph=False)  # noqa: E731
     else:
         raise SystemExit(f"unknown --profile-op {op}")
     for _ in range(steps):
