@@ -480,6 +480,20 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
     print(f"profile-op {op}: {steps} runs ok")
 
 
+def all_reduce_max(dist, torch, v: float, device: str) -> float:
+    """The maximum of v over the ranks of the default process group."""
+    t = torch.tensor([v], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(ms_total: float, steps: int, world: int, bytes_per_step: float, reduce_max):
+    """Whole-job GB/s: every rank processes bytes_per_step per step (weak
+    scaling); the job's time is the slowest rank's. Returns (GB/s, ms/step)."""
+    ms_step = reduce_max(ms_total) / steps
+    return world * bytes_per_step / (ms_step * 1e-3) / 1e9, ms_step
+
+
 def omp_threads() -> int:
     try:
         return int(os.environ.get("OMP_NUM_THREADS", "")) or os.cpu_count() or 1
@@ -523,6 +537,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--headline-only", action="store_true", help="skip the per-op measurements of the other workloads")
+    ap.add_argument("--only", default=None, choices=["c1", "c3", "c4", "c5"],
+                    help="measure one per-op workload and print its figures (no headline line)")
     ap.add_argument("--profile-op", default=None, help="run one op --steps times for a profiler capture")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -532,6 +548,15 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.only:
+        import torch
+        import ncarray_gb300 as nca
+        peak, _ = peaks()
+        flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device="cuda") if args.only == "c1" else None
+        fn = {"c1": lambda: measure_c1(torch, nca, peak, flush_buf), "c3": lambda: measure_c3(torch, nca, peak),
+              "c4": lambda: measure_c4(torch, nca, peak), "c5": lambda: measure_c5(torch, nca, peak)}[args.only]
+        print(json.dumps({args.only: fn()}), flush=True)
         return
 
     import torch
@@ -600,12 +625,8 @@ def main():
     ms_fused = time_events(torch, g_fused.replay, args.steps)
     ms_int = time_events(torch, g_int.replay, args.steps)
     clocks = sampler.stop()
-    if dist:
-        t = torch.tensor([ms_total], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms_step = ms_total / args.steps
-    value = world * by["step"] / (ms_step * 1e-3) / 1e9
+    value, ms_step = job_throughput(ms_total, args.steps, world, by["step"],
+                                    (lambda v: all_reduce_max(dist, torch, v, "cuda")) if dist else (lambda v: v))
     peak, peak_kind = peaks()
     fused_gbs = by["fused"] / (ms_fused * 1e-3) / 1e9
     int_gbs = by["int"] / (ms_int * 1e-3) / 1e9

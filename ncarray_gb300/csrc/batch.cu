@@ -8,16 +8,18 @@
 //   - nca_batch_create splits every array into chunks of `chunk_bytes` and
 //     uploads a descriptor table (array, first element, element count) once;
 //   - the persistent kernel's CTAs walk the chunk table with a static stride
-//     (chunks carry equal bytes, so the walk is balanced); each CTA reduces its
-//     chunk with per-thread float-float sums (Knuth TwoSum) of x and of
-//     fma(x, x, -x), a float max, and a float64 block tree, then writes one
-//     partial record;
+//     (chunks carry equal bytes, so the walk is balanced), streaming each
+//     chunk through shared memory by bulk copies; each CTA reduces its chunk
+//     with per-thread float-float sums (Knuth TwoSum, packed float32x2) of x
+//     and of fma(x, x, -x), a float max, and a float64 block tree, then
+//     writes one partial record;
 //   - the CTA finishing the last chunk of an array (a per-array counter
 //     incremented after a release fence) combines that array's partials in
 //     chunk order (deterministic) and resets the counter for the next launch.
-// There is no waiting anywhere, so nothing can hang. The schedule (chunk
-// bytes, threads, unroll, CTAs per SM) comes from an autotuner whose choices are
-// cached per shape class in a text file next to the JIT cache.
+// The only waits are the bounded mbarrier waits of the bulk-copy pipeline
+// (below). The schedule (chunk bytes, slab bytes, CTAs per SM) comes from an
+// autotuner whose choices are cached per shape class in a text file next to
+// the JIT cache.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,10 +43,11 @@ struct nca_batch {
   void* d_chunks = nullptr;   // ChunkDev[nchunks]
   void* d_parts = nullptr;    // PartDev[nchunks]
   void* d_done = nullptr;     // unsigned[n]
+  void* d_status = nullptr;   // int: NCA_ERR_TIMEOUT after a wait that ran out
   long long nchunks = 0;
   // schedule
   long long chunk_bytes = 256 * 1024;
-  int threads = 256, unroll = 4, ctas_per_sm = 4;
+  int threads = 256, slab = 16384, ctas_per_sm = 3;
   std::string shape_class;
   // graph
   cudaGraphExec_t graph = nullptr;
@@ -68,6 +71,8 @@ struct ChunkDev {
   int index;        // chunk number within the item
   long long begin;  // first element
   long long count;  // elements
+  unsigned long long a, e;   // byte range of the 16-byte aligned body (a == e: none)
+  long long slabs;           // bulk-copy slabs of the body
 };
 
 struct PartDev {
@@ -159,46 +164,80 @@ template <> struct Vec<NCA_FLOAT16> {
   }
 };
 
-// Reduces chunk c of its item into a PartDev (valid in thread 0): a scalar head
-// up to the first 16-byte boundary, UNROLL 16-byte loads in flight per thread
-// over the aligned body, then a scalar tail.
-template <int DT, int UNROLL>
-__device__ PartDev reduce_chunk_t(const ItemDev& it, const ChunkDev& c) {
-  using V = Vec<DT>;
-  constexpr int isz = DT == NCA_FLOAT32 ? 4 : 2;
-  Acc2 acc;
+// ---- the persistent kernel --------------------------------------------------------
+// Every CTA walks its chunks (blockIdx.x, + gridDim.x, ...). A chunk's 16-byte
+// aligned body streams through NSLAB shared-memory slabs of `slab` bytes filled
+// by cp.async.bulk (thread 0 keeps NSLAB slabs in flight, across chunk
+// boundaries, completion on one mbarrier per slab); the unaligned head and
+// tail (< 16 bytes each) are read with plain loads. Waits are bounded (2 s of
+// %globaltimer): on a timeout the CTA records NCA_ERR_TIMEOUT in the batch
+// status word, waits (bounded) for its copies in flight and stops.
+constexpr int NSLAB = 4;
+constexpr unsigned long long kWaitNs = 2000000000ull;
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    if (ok) return true;
+    if (gtimer() - t0 > limit_ns) return false;
+  }
+}
+
+// the 16-byte aligned body of a chunk (computed on the host)
+struct Body {
+  uintptr_t a, e;
+  long long slabs;
+};
+__device__ __forceinline__ Body chunk_body(const ChunkDev& c) { return Body{(uintptr_t)c.a, (uintptr_t)c.e, c.slabs}; }
+
+// elements of 16 bytes: float32 gives 2 pairs, 16-bit types 4
+template <int DT>
+__device__ __forceinline__ void see_vec(Acc2& acc, const uint4& u) {
+  float2 f[Vec<DT>::kElems / 2];
+  Vec<DT>::unpack(u, f);
+#pragma unroll
+  for (int j = 0; j < Vec<DT>::kElems / 2; ++j) acc.see(f[j]);
+}
+
+// two accumulator sets take alternate vectors: two independent TwoSum chains
+template <int DT>
+__device__ __forceinline__ void see_slab(Acc2& a0, Acc2& a1, const uint4* v, int nv) {
   const int T = blockDim.x;
-  const char* base = static_cast<const char*>(it.data);
-  const long long b = c.begin, e = c.begin + c.count;
-  const uintptr_t a0 = (uintptr_t)(base + b * isz);
-  long long head = (long long)(((16 - (a0 & 15)) & 15) / isz);
-  if (head > c.count) head = c.count;
-  const long long nv = (c.count - head) / V::kElems;          // aligned 16-byte vectors
-  const long long vb = b + head, ve = vb + nv * V::kElems;
-  if (threadIdx.x < head) acc.see(make_float2(V::one(it.data, b + threadIdx.x), 0.f), false);
-  const uint4* vp = reinterpret_cast<const uint4*>(base + vb * isz);
-  long long i = threadIdx.x;
-  for (; i + (long long)(UNROLL - 1) * T < nv; i += (long long)UNROLL * T) {
-    uint4 u[UNROLL];
-#pragma unroll
-    for (int k = 0; k < UNROLL; ++k) u[k] = __ldcs(vp + i + (long long)k * T);
-#pragma unroll
-    for (int k = 0; k < UNROLL; ++k) {
-      float2 f[V::kElems / 2];
-      V::unpack(u[k], f);
-#pragma unroll
-      for (int j = 0; j < V::kElems / 2; ++j) acc.see(f[j]);
-    }
+  int i = threadIdx.x;
+  for (; i + T < nv; i += 2 * T) {
+    const uint4 u0 = v[i], u1 = v[i + T];
+    see_vec<DT>(a0, u0);
+    see_vec<DT>(a1, u1);
   }
-  for (; i < nv; i += T) {
-    float2 f[V::kElems / 2];
-    V::unpack(__ldcs(vp + i), f);
-#pragma unroll
-    for (int j = 0; j < V::kElems / 2; ++j) acc.see(f[j]);
+  if (i < nv) see_vec<DT>(a0, v[i]);
+}
+
+// head and tail elements of chunk c outside its aligned body
+__device__ __forceinline__ void see_edges(Acc2& acc, const ItemDev& it, const ChunkDev& c, const Body& b) {
+  const int isz = it.dtype == NCA_FLOAT32 ? 4 : 2;
+  const uintptr_t lo = (uintptr_t)it.data + (uintptr_t)(c.begin * isz);
+  const long long nh = (long long)((b.a - lo) / isz);               // elements before the body
+  const long long nt = c.count - nh - (long long)((b.e - b.a) / isz);  // elements after it
+  for (long long t = threadIdx.x; t < nh + nt; t += blockDim.x) {
+    const long long i = t < nh ? c.begin + t : c.begin + c.count - nt + (t - nh);
+    acc.see(make_float2(ld_elem(it.data, i, it.dtype), 0.f), false);
   }
-  for (long long t = ve + threadIdx.x; t < e; t += T) acc.see(make_float2(V::one(it.data, t), 0.f), false);
-  double ds = acc.s.get(), dq = acc.q.get();
-  float mx = acc.mx;
+}
+
+// block tree of a chunk's accumulators into a PartDev (valid in thread 0)
+__device__ PartDev block_part(const Acc2& acc, const Acc2& acc1) {
+  double ds = acc.s.get() + acc1.s.get(), dq = acc.q.get() + acc1.q.get();
+  float mx = fmaxf(acc.mx, acc1.mx);
   for (int off = 16; off > 0; off >>= 1) {
     ds += __shfl_down_sync(0xffffffffu, ds, off);
     dq += __shfl_down_sync(0xffffffffu, dq, off);
@@ -206,7 +245,7 @@ __device__ PartDev reduce_chunk_t(const ItemDev& it, const ChunkDev& c) {
   }
   __shared__ double sh_s[32], sh_q[32];
   __shared__ float sh_m[32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (T + 31) >> 5;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
   __syncthreads();
   if (lane == 0) { sh_s[wid] = ds; sh_q[wid] = dq; sh_m[wid] = mx; }
   __syncthreads();
@@ -221,22 +260,70 @@ __device__ PartDev reduce_chunk_t(const ItemDev& it, const ChunkDev& c) {
   return p;
 }
 
-template <int UNROLL>
-__device__ PartDev reduce_chunk(const ItemDev& it, const ChunkDev& c) {
-  if (it.dtype == NCA_FLOAT32) return reduce_chunk_t<NCA_FLOAT32, UNROLL>(it, c);
-  if (it.dtype == NCA_BFLOAT16) return reduce_chunk_t<NCA_BFLOAT16, UNROLL>(it, c);
-  return reduce_chunk_t<NCA_FLOAT16, UNROLL>(it, c);
-}
-
-template <int UNROLL>
 __global__ void batch_persistent_kernel(const ItemDev* __restrict__ items, const ChunkDev* __restrict__ chunks,
                                         long long nchunks, PartDev* __restrict__ parts, unsigned* __restrict__ done,
-                                        nca_batch_result* __restrict__ results) {
+                                        nca_batch_result* __restrict__ results, int slab, int* __restrict__ status) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+  const uint32_t bbase = sbase + NSLAB * slab;
   __shared__ int s_last;
-  for (long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < NSLAB; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bbase + 8 * k) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  // producer cursor (thread 0): next (chunk, slab) to issue and slabs issued
+  long long pc = blockIdx.x, ps = 0, issued = 0;
+  Body pb{0, 0, 0};
+  if (threadIdx.x == 0 && pc < nchunks) pb = chunk_body(chunks[pc]);
+  auto advance = [&]() {   // to the next slab of this CTA's sequence, if any
+    while (pc < nchunks) {
+      if (ps < pb.slabs) return true;
+      pc += gridDim.x;
+      ps = 0;
+      if (pc < nchunks) pb = chunk_body(chunks[pc]);
+    }
+    return false;
+  };
+  auto issue = [&]() {
+    const Body& bd = pb;
+    const uintptr_t src = bd.a + (uintptr_t)ps * slab;
+    const uintptr_t left = bd.e - src;
+    const uint32_t bytes = (uint32_t)(left < (uintptr_t)slab ? left : (uintptr_t)slab);
+    const int k = (int)(issued % NSLAB);
+    const uint32_t bar = bbase + 8 * k;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(sbase + (uint32_t)(k * slab)), "l"(src), "r"(bytes), "r"(bar) : "memory");
+    ++issued;
+    ++ps;
+  };
+  if (threadIdx.x == 0)
+    for (int k = 0; k < NSLAB && advance(); ++k) issue();
+  long long consumed = 0;
+  bool failed = false;
+  for (long long c = blockIdx.x; c < nchunks && !failed; c += gridDim.x) {
     const ChunkDev ch = chunks[c];
     const ItemDev it = items[ch.item];
-    const PartDev p = reduce_chunk<UNROLL>(it, ch);
+    const Body bd = chunk_body(ch);
+    Acc2 acc, acc1;
+    see_edges(acc, it, ch, bd);
+    for (long long i = 0; i < bd.slabs; ++i, ++consumed) {
+      const int k = (int)(consumed % NSLAB);
+      const bool ok = mbar_wait(bbase + 8 * k, (uint32_t)((consumed / NSLAB) & 1), kWaitNs);
+      if (__syncthreads_or(ok ? 0 : 1)) { failed = true; break; }
+      const uintptr_t src = bd.a + (uintptr_t)i * slab;
+      const uintptr_t left = bd.e - src;
+      const int nv = (int)((left < (uintptr_t)slab ? left : (uintptr_t)slab) / 16);
+      const uint4* v = reinterpret_cast<const uint4*>(sm + k * slab);
+      if (it.dtype == NCA_FLOAT32) see_slab<NCA_FLOAT32>(acc, acc1, v, nv);
+      else if (it.dtype == NCA_BFLOAT16) see_slab<NCA_BFLOAT16>(acc, acc1, v, nv);
+      else see_slab<NCA_FLOAT16>(acc, acc1, v, nv);
+      __syncthreads();   // slab k is free again
+      if (threadIdx.x == 0 && advance()) issue();
+    }
+    if (failed) break;
+    const PartDev p = block_part(acc, acc1);
     if (threadIdx.x == 0) {
       parts[c] = p;
       __threadfence();
@@ -264,6 +351,11 @@ __global__ void batch_persistent_kernel(const ItemDev* __restrict__ items, const
       done[ch.item] = 0u;   // ready for the next launch
     }
     __syncthreads();
+  }
+  if (failed && threadIdx.x == 0) {
+    atomicExch(status, (int)NCA_ERR_TIMEOUT);
+    for (long long k = consumed; k < issued; ++k)
+      mbar_wait(bbase + 8 * (int)(k % NSLAB), (uint32_t)((k / NSLAB) & 1), kWaitNs / 2);
   }
 }
 
@@ -321,12 +413,11 @@ void launch_persistent(nca_batch* B, nca_batch_result* results, cudaStream_t s) 
   const ChunkDev* ch = (const ChunkDev*)B->d_chunks;
   PartDev* pa = (PartDev*)B->d_parts;
   unsigned* dn = (unsigned*)B->d_done;
-  switch (B->unroll) {
-    case 1: batch_persistent_kernel<1><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
-    case 2: batch_persistent_kernel<2><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
-    case 8: batch_persistent_kernel<8><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
-    default: batch_persistent_kernel<4><<<grid, B->threads, 0, s>>>(it, ch, B->nchunks, pa, dn, results); break;
-  }
+  const int smem = NSLAB * B->slab + 8 * NSLAB;
+  nca::check_cuda(cudaFuncSetAttribute(batch_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+                  "batch smem");
+  batch_persistent_kernel<<<grid, B->threads, smem, s>>>(it, ch, B->nchunks, pa, dn, results, B->slab,
+                                                         (int*)B->d_status);
   nca::check_cuda(cudaGetLastError(), "batched kernel launch");
   nca::count_launch();
 }
@@ -353,7 +444,17 @@ void build_chunks(nca_batch* B, cudaStream_t s) {
     items[i].first_chunk = (int)chunks.size();
     long long k = 0;
     for (long long b = 0; b < src.length || (b == 0 && src.length == 0); b += per, ++k) {
-      ChunkDev c{i, (int)k, b, std::min(per, src.length - b)};
+      ChunkDev c{i, (int)k, b, std::min(per, src.length - b), 0, 0, 0};
+      // the 16-byte aligned part of the chunk's bytes, moved by bulk copies
+      const uintptr_t lo = (uintptr_t)src.data + (uintptr_t)(c.begin * isz), hi = lo + (uintptr_t)(c.count * isz);
+      const uintptr_t a = (lo + 15) & ~(uintptr_t)15, e = hi & ~(uintptr_t)15;
+      if (e > a) {
+        c.a = a;
+        c.e = e;
+        c.slabs = (long long)((e - a + B->slab - 1) / B->slab);
+      } else {
+        c.a = c.e = lo;
+      }
       chunks.push_back(c);
       if (src.length == 0) break;
     }
@@ -366,6 +467,10 @@ void build_chunks(nca_batch* B, cudaStream_t s) {
   if (!B->d_done) {
     check_cuda(cudaMalloc(&B->d_done, sizeof(unsigned) * std::max(B->n, 1)), "batch counters");
     check_cuda(cudaMemsetAsync(B->d_done, 0, sizeof(unsigned) * std::max(B->n, 1), s), "batch counters");
+  }
+  if (!B->d_status) {
+    check_cuda(cudaMalloc(&B->d_status, sizeof(int)), "batch status");
+    check_cuda(cudaMemsetAsync(B->d_status, 0, sizeof(int), s), "batch status");
   }
   check_cuda(cudaMalloc(&B->d_chunks, sizeof(ChunkDev) * std::max<long long>(B->nchunks, 1)), "batch chunks");
   check_cuda(cudaMalloc(&B->d_parts, sizeof(PartDev) * std::max<long long>(B->nchunks, 1)), "batch partials");
@@ -389,17 +494,23 @@ std::string shape_class(const nca_batch* B) {
   return os.str();
 }
 
-std::string tune_file() { return nca::jit_cache_dir() + "/batch_tune.txt"; }
+// lines "<shape class> <chunk bytes> <threads> <slab bytes> <ctas per sm>"
+std::string tune_file() { return nca::jit_cache_dir() + "/batch_tune_bulk.txt"; }
+
+bool schedule_ok(long long cb, int th, int slab, int cps) {
+  return cb >= (64ll << 10) && (th == 256 || th == 512) && (slab == 8192 || slab == 16384 || slab == 32768) &&
+         cps >= 1 && cps <= 8 && (long long)cps * NSLAB * slab <= 200ll * 1024 && th * cps <= 2048;
+}
 
 bool load_tuned(nca_batch* B) {
   std::ifstream f(tune_file());
   std::string key;
   long long cb;
-  int th, un, cps;
+  int th, sl, cps;
   bool found = false;
-  while (f >> key >> cb >> th >> un >> cps) {
-    if (key == B->shape_class) {
-      B->chunk_bytes = cb; B->threads = th; B->unroll = un; B->ctas_per_sm = cps;
+  while (f >> key >> cb >> th >> sl >> cps) {
+    if (key == B->shape_class && schedule_ok(cb, th, sl, cps)) {
+      B->chunk_bytes = cb; B->threads = th; B->slab = sl; B->ctas_per_sm = cps;
       found = true;
     }
   }
@@ -408,7 +519,7 @@ bool load_tuned(nca_batch* B) {
 
 void store_tuned(const nca_batch* B) {
   std::ofstream f(tune_file(), std::ios::app);
-  if (f) f << B->shape_class << " " << B->chunk_bytes << " " << B->threads << " " << B->unroll << " "
+  if (f) f << B->shape_class << " " << B->chunk_bytes << " " << B->threads << " " << B->slab << " "
            << B->ctas_per_sm << "\n";
 }
 
@@ -509,20 +620,19 @@ int32_t nca_batch_autotune(nca_batch* B, nca_batch_result* results, void* stream
     using namespace nca;
     if (!B || !results) fail(NCA_ERR_INVALID, "null argument");
     cudaStream_t s = (cudaStream_t)stream;
-    struct Cand { long long cb; int th, un, cps; };
+    struct Cand { long long cb; int th, sl, cps; };
     std::vector<Cand> cands;
-    for (long long cb : {128ll << 10, 256ll << 10, 512ll << 10, 1024ll << 10})
-      for (int th : {256, 512})
-        for (int un : {4, 8})
-          for (int cps : {2, 4})
-            if (th * cps <= 2048) cands.push_back({cb, th, un, cps});
+    for (long long cb : {256ll << 10, 512ll << 10, 1024ll << 10})
+      for (int sl : {8192, 16384, 32768})
+        for (int cps : {2, 3, 4})
+          if (schedule_ok(cb, 256, sl, cps)) cands.push_back({cb, 256, sl, cps});
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "event");
     check_cuda(cudaEventCreate(&e1), "event");
     float best = 1e30f;
     Cand bestc = cands[0];
     for (const auto& c : cands) {
-      B->chunk_bytes = c.cb; B->threads = c.th; B->unroll = c.un; B->ctas_per_sm = c.cps;
+      B->chunk_bytes = c.cb; B->threads = c.th; B->slab = c.sl; B->ctas_per_sm = c.cps;
       build_chunks(B, s);
       launch_persistent(B, results, s);   // warm-up
       check_cuda(cudaEventRecord(e0, s), "record");
@@ -535,7 +645,7 @@ int32_t nca_batch_autotune(nca_batch* B, nca_batch_result* results, void* stream
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    B->chunk_bytes = bestc.cb; B->threads = bestc.th; B->unroll = bestc.un; B->ctas_per_sm = bestc.cps;
+    B->chunk_bytes = bestc.cb; B->threads = bestc.th; B->slab = bestc.sl; B->ctas_per_sm = bestc.cps;
     build_chunks(B, s);
     store_tuned(B);
   });
@@ -547,7 +657,7 @@ int32_t nca_batch_schedule(const nca_batch* B, int64_t* chunk, int32_t* threads,
     if (!B) nca::fail(NCA_ERR_INVALID, "null batch");
     if (chunk) *chunk = B->chunk_bytes;
     if (threads) *threads = B->threads;
-    if (items_per_thread) *items_per_thread = B->unroll;
+    if (items_per_thread) *items_per_thread = B->slab / (16 * B->threads);   // 16-byte vectors per thread per slab
     if (ctas) *ctas = (int32_t)std::min<long long>(B->nchunks, (long long)nca::sm_count(B->dev) * B->ctas_per_sm);
   });
 }
@@ -555,10 +665,13 @@ int32_t nca_batch_schedule(const nca_batch* B, int64_t* chunk, int32_t* threads,
 int32_t nca_batch_status(nca_batch* B, int32_t* status, void* stream) {
   return nca::guarded([&] {
     if (!B || !status) nca::fail(NCA_ERR_INVALID, "null argument");
-    // the persistent kernel never waits on another CTA, so it has no timeout
-    // path: the status is that of the stream
-    nca::check_cuda(cudaStreamSynchronize((cudaStream_t)stream), "batch stream");
-    *status = 0;
+    // NCA_ERR_TIMEOUT if a bounded wait of the pipeline gave up (read and cleared)
+    cudaStream_t s = (cudaStream_t)stream;
+    int v = 0;
+    nca::check_cuda(cudaMemcpyAsync(&v, B->d_status, sizeof(int), cudaMemcpyDeviceToHost, s), "batch status");
+    nca::check_cuda(cudaMemsetAsync(B->d_status, 0, sizeof(int), s), "batch status");
+    nca::check_cuda(cudaStreamSynchronize(s), "batch stream");
+    *status = v;
   });
 }
 
@@ -567,6 +680,7 @@ void nca_batch_destroy(nca_batch* B) {
   free_tables(B);
   if (B->d_items) cudaFree(B->d_items);
   if (B->d_done) cudaFree(B->d_done);
+  if (B->d_status) cudaFree(B->d_status);
   if (B->capture_stream) cudaStreamDestroy(B->capture_stream);
   delete B;
 }
