@@ -92,7 +92,12 @@ __device__ __forceinline__ T fmaT(T a, T b, T c) {
   if constexpr (sizeof(T) == 4) return __fmaf_rn(a, b, c); else return __fma_rn(a, b, c);
 }
 
-template <class T, bool STAR7>
+// MODE 0: any 27 weights; 1: 7-point star (weights of offsets with two or
+// three non-zero components are zero); 2: isotropic 27-point (the weight of an
+// offset depends only on how many of its components are non-zero: w[13] for
+// none, w[12] for one, w[9] for two, w[0] for three), evaluated per plane from
+// the in-plane centre, face and corner sums (12 instead of 27 FMAs a point).
+template <class T, int MODE>
 __global__ void __launch_bounds__(THREADS)
 stencil_tma_kernel(const __grid_constant__ CUtensorMap tmap, T* __restrict__ out, int nx, int ny, int nz,
                    int zt, const __grid_constant__ Weights<T> W) {
@@ -133,7 +138,7 @@ stencil_tma_kernel(const __grid_constant__ CUtensorMap tmap, T* __restrict__ out
       const int c0 = HX + tx4;
       T v[3][6];
       load_row(plane + (ty + 1) * BW, c0, v[1]);
-      if constexpr (STAR7) {
+      if constexpr (MODE == 1) {
 #pragma unroll
         for (int r = 0; r < 3; r += 2) {
           const T* row = plane + (ty + r) * BW;
@@ -154,7 +159,16 @@ stencil_tma_kernel(const __grid_constant__ CUtensorMap tmap, T* __restrict__ out
       T pm[4], p0[4], pp[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        if constexpr (STAR7) {
+        if constexpr (MODE == 2) {
+          // in-plane centre C, faces F and corners K of output column j
+          const T C = v[1][j + 1];
+          const T F = ((v[1][j] + v[1][j + 2]) + v[0][j + 1]) + v[2][j + 1];
+          const T K = (v[0][j] + v[0][j + 2]) + (v[2][j] + v[2][j + 2]);
+          p0[j] = fmaT(W.w[9], K, fmaT(W.w[12], F, W.w[13] * C));
+          const T q = fmaT(W.w[0], K, fmaT(W.w[9], F, W.w[12] * C));
+          pm[j] = q;
+          pp[j] = q;
+        } else if constexpr (MODE == 1) {
           pm[j] = W.w[4] * v[1][j + 1];
           pp[j] = W.w[22] * v[1][j + 1];
           T s = W.w[13] * v[1][j + 1];
@@ -281,6 +295,17 @@ bool star7(const double* w) {
   return true;
 }
 
+// the weight of every offset depends only on its number of non-zero components
+bool isotropic27(const double* w) {
+  const double cls[4] = {w[13], w[12], w[9], w[0]};
+  for (int i = 0; i < 27; ++i) {
+    const int dz = i / 9, oy = (i / 3) % 3, ox = i % 3;
+    const int nz = (dz != 1) + (oy != 1) + (ox != 1);
+    if (w[i] != cls[nz]) return false;
+  }
+  return true;
+}
+
 bool tma_ok(const Grid3& g) {
   // row pitch and plane pitch must be multiples of 16 bytes and the x extent a
   // multiple of 4 (each thread stores 4 aligned outputs)
@@ -301,7 +326,7 @@ void encode_map(CUtensorMap* m, const Grid3& g) {
 }
 
 template <class T>
-void launch_one(const Grid3& src, const Grid3& dst, const Weights<T>& W, bool s7, cudaStream_t s) {
+void launch_one(const Grid3& src, const Grid3& dst, const Weights<T>& W, int mode, cudaStream_t s) {
   using namespace nca;
   const int dev = current_device();
   if (tma_ok(src) && tma_ok(dst)) {
@@ -310,11 +335,12 @@ void launch_one(const Grid3& src, const Grid3& dst, const Weights<T>& W, bool s7
     const int zt = src.nz >= 256 ? 32 : (src.nz >= 64 ? 16 : 8);
     dim3 grid((src.nx + TX - 1) / TX, (src.ny + TY - 1) / TY, (src.nz + zt - 1) / zt);
     const size_t smem = NST * stage_bytes<T>() + NST * 8;
-    if (s7) {
-      stencil_tma_kernel<T, true><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
-    } else {
-      stencil_tma_kernel<T, false><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
-    }
+    if (mode == 1)
+      stencil_tma_kernel<T, 1><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
+    else if (mode == 2)
+      stencil_tma_kernel<T, 2><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
+    else
+      stencil_tma_kernel<T, 0><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
   } else {
     const long long n = (long long)src.nx * src.ny * src.nz;
     const long long blocks = std::min<long long>((n + THREADS - 1) / THREADS, (long long)sm_count(dev) * 32);
@@ -335,12 +361,12 @@ void run(const nca_view* a, const nca_view* b, const double* w27, double dt, int
   const size_t bytes = (size_t)ga.nx * ga.ny * ga.nz * dtinfo(ga.dtype).size;
   const char *pa = (const char*)ga.base, *pb = (const char*)gb.base;
   if (pa < pb + bytes && pb < pa + bytes) fail(NCA_ERR_INVALID, "stencil source and destination overlap");
-  const bool s7 = star7(w27);
+  const int mode = star7(w27) ? 1 : isotropic27(w27) ? 2 : 0;
   for (int it = 0; it < iters; ++it) {
     const Grid3& src = (it % 2 == 0) ? ga : gb;
     const Grid3& dst = (it % 2 == 0) ? gb : ga;
-    if (ga.dtype == NCA_FLOAT32) launch_one<float>(src, dst, make_weights<float>(w27, dt), s7, s);
-    else launch_one<double>(src, dst, make_weights<double>(w27, dt), s7, s);
+    if (ga.dtype == NCA_FLOAT32) launch_one<float>(src, dst, make_weights<float>(w27, dt), mode, s);
+    else launch_one<double>(src, dst, make_weights<double>(w27, dt), mode, s);
   }
 }
 

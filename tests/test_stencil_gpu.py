@@ -38,13 +38,16 @@ def test_stencil_f64(cuda, orc, shape, kind):
 
 
 @pytest.mark.parametrize("shape", SHAPES[:3])
-@pytest.mark.parametrize("kind", ["7", "27"])
+@pytest.mark.parametrize("kind", ["7", "27", "random"])
 def test_stencil_f32_error_vs_f64(cuda, orc, shape, kind):
+    """7-point (star kernel), isotropic 27-point (centre/face/corner sums) and
+    arbitrary 27 weights (general kernel)."""
     rng = np.random.default_rng(SEED + 3)
     u = rng.normal(size=shape).astype(np.float32)
-    w = (laplacian7() if kind == "7" else laplacian27()).reshape(27)
-    ref = orc.stencil3d_f64(u.astype(np.float64), w, 0.1, 10)
-    got = run(u, w, 0.1, 10, np.float32).astype(np.float64)
+    w = {"7": laplacian7(), "27": laplacian27(), "random": rng.normal(size=(3, 3, 3)) / 8}[kind].reshape(27)
+    iters = 3 if kind == "random" else 10
+    ref = orc.stencil3d_f64(u.astype(np.float64), w, 0.1, iters)
+    got = run(u, w, 0.1, iters, np.float32).astype(np.float64)
     rel_l2 = np.linalg.norm(got - ref) / np.linalg.norm(ref)
     assert rel_l2 <= 2e-6, rel_l2
     assert np.max(np.abs(got - ref)) <= 1e-5 * np.max(np.abs(ref))
