@@ -184,6 +184,15 @@ int32_t nca_reduce_noalloc(const nca_view* src, int32_t op, const nca_view* out,
  * (gpuengine.hh:377-637; kernels.cuh:613-644). */
 int32_t nca_copy(const nca_view* src, const nca_view* dst, void* stream);
 
+/* Host <-> device copy of two views of equal shape and dtype (either may be the
+ * host side; pinned host memory makes it asynchronous on `stream`), each
+ * contiguous along its innermost axis with positive strides: the outer axes
+ * become 2-D copies, no staging kernel. Replaces the host/device transfers of
+ * GPUEngine::execute_copy_into (gpuengine.hh:378-510; to_host / to_device,
+ * binding_builder.hh:543-591), which copy synchronously and pack strided
+ * views through a kernel first. */
+int32_t nca_copy_host(const nca_view* src, const nca_view* dst, void* stream);
+
 /* dst[...] = cast(scalar): GPUEngine::execute_fill (gpuengine.hh:338-376). */
 int32_t nca_fill(const nca_view* dst, int32_t scalar_dtype, const void* scalar, void* stream);
 

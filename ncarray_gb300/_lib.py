@@ -78,6 +78,7 @@ EXPORTS = {
     "nca_reduce": (c_int32, [POINTER(View), c_int32, c_uint32, POINTER(View), c_void_p]),
     "nca_reduce_noalloc": (c_int32, [POINTER(View), c_int32, POINTER(View), c_void_p]),
     "nca_copy": (c_int32, [POINTER(View), POINTER(View), c_void_p]),
+    "nca_copy_host": (c_int32, [POINTER(View), POINTER(View), c_void_p]),
     "nca_fill": (c_int32, [POINTER(View), c_int32, c_void_p, c_void_p]),
     "nca_stencil3d": (c_int32, [POINTER(View), POINTER(View), POINTER(c_double), c_double, c_void_p]),
     "nca_stencil3d_iterate": (c_int32, [POINTER(View), POINTER(View), POINTER(c_double), c_double, c_int32, c_void_p]),

@@ -145,6 +145,37 @@ class NCDevArray:
         raw = src._buf[src._offset: src._offset + src.nbytes].cpu().numpy()
         return raw.view(npdt).reshape(self.shape)
 
+    # ---- host <-> device copies of views (nca_copy_host) ----
+    def _host_view(self, host) -> _lib.View:
+        """A View of a host numpy array or CPU torch tensor with this array's
+        shape and itemsize (pinned torch memory makes the copy asynchronous)."""
+        if isinstance(host, np.ndarray):
+            ptr, itemsize, strides = host.ctypes.data, host.itemsize, tuple(host.strides)
+        else:
+            if host.is_cuda:
+                raise TypeError("host buffer expected")
+            itemsize = host.element_size()
+            ptr, strides = host.data_ptr(), tuple(st * itemsize for st in host.stride())
+        if tuple(host.shape) != tuple(self.shape) or itemsize != self.itemsize:
+            raise ValueError(f"host buffer {tuple(host.shape)} x {itemsize} B does not match {self.shape} x "
+                             f"{self.itemsize} B")
+        return _lib.make_view(ptr, self.dtype, self.shape, strides)
+
+    def copy_from(self, host, stream=None) -> "NCDevArray":
+        """self[...] = host (same shape and itemsize) on `stream` (default: the
+        current stream); both views contiguous along their innermost axis."""
+        hv = self._host_view(host)
+        _lib.call("nca_copy_host", ctypes.byref(hv), ctypes.byref(self.view_struct()),
+                  current_stream() if stream is None else stream)
+        return self
+
+    def copy_to(self, host, stream=None) -> None:
+        """host[...] = self (same shape and itemsize) on `stream`; asynchronous
+        with pinned host memory (synchronise before reading it)."""
+        hv = self._host_view(host)
+        _lib.call("nca_copy_host", ctypes.byref(self.view_struct()), ctypes.byref(hv),
+                  current_stream() if stream is None else stream)
+
     def __array__(self, dtype=None, copy=None):
         a = self.to_host()
         return a.astype(dtype) if dtype is not None else a
@@ -478,6 +509,37 @@ class DevExpr:
         _lib.call("nca_expr_reduce", ctypes.byref(t), ops, n,
                   ctypes.byref(out.view_struct()) if out is not None else None, rarr, len(rs), stream)
         return results
+
+    # ---- host <-> device copies of views (nca_copy_host) ----
+    def _host_view(self, host) -> _lib.View:
+        """A View of a host numpy array or CPU torch tensor with this array's
+        shape and itemsize (pinned torch memory makes the copy asynchronous)."""
+        if isinstance(host, np.ndarray):
+            ptr, itemsize, strides = host.ctypes.data, host.itemsize, tuple(host.strides)
+        else:
+            if host.is_cuda:
+                raise TypeError("host buffer expected")
+            itemsize = host.element_size()
+            ptr, strides = host.data_ptr(), tuple(st * itemsize for st in host.stride())
+        if tuple(host.shape) != tuple(self.shape) or itemsize != self.itemsize:
+            raise ValueError(f"host buffer {tuple(host.shape)} x {itemsize} B does not match {self.shape} x "
+                             f"{self.itemsize} B")
+        return _lib.make_view(ptr, self.dtype, self.shape, strides)
+
+    def copy_from(self, host, stream=None) -> "NCDevArray":
+        """self[...] = host (same shape and itemsize) on `stream` (default: the
+        current stream); both views contiguous along their innermost axis."""
+        hv = self._host_view(host)
+        _lib.call("nca_copy_host", ctypes.byref(hv), ctypes.byref(self.view_struct()),
+                  current_stream() if stream is None else stream)
+        return self
+
+    def copy_to(self, host, stream=None) -> None:
+        """host[...] = self (same shape and itemsize) on `stream`; asynchronous
+        with pinned host memory (synchronise before reading it)."""
+        hv = self._host_view(host)
+        _lib.call("nca_copy_host", ctypes.byref(self.view_struct()), ctypes.byref(hv),
+                  current_stream() if stream is None else stream)
 
     def __array__(self, dtype=None, copy=None):
         return self.materialize().__array__(dtype)
