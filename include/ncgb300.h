@@ -80,12 +80,18 @@ typedef enum nca_reduce_op {
 
 /*
  * An N-d view: NCOffsetsPolicy semantics (src/lib/ncarray/layout.hh:451-535).
- * Element address = data + sum_k (idx_k * strides[k] + offsets[k]) for every
- * axis k, except that on `pointer_axis` (if >= 0) the running pointer is read
- * as a void* table: p = ((void**)p)[idx + offsets[axis] / sizeof(void*)]...
- * (pointer axes are rejected with NCA_ERR_UNSUPPORTED by this build).
- * Strides and offsets are in BYTES; stride 0 broadcasts an axis.
+ * Element address = data + sum_k (idx_k * strides[k] + offsets[k]) over the
+ * axes k, walked in order, except that on `pointer_axis` (if >= 0) the running
+ * pointer p is read as a void* table: p = ((void* const*)p)[idx + offsets[axis]]
+ * (offsets[pointer_axis] is an index offset), so axes before the pointer axis
+ * move the table pointer and later axes move the panel pointer.
+ * With flags = NCA_VIEW_SUBOFFSETS the pointer axis has PEP 3118 suboffset
+ * semantics instead (SOArrayPolicy, layout.hh:677-778): p += idx * strides[axis],
+ * then p = *(void**)p + offsets[axis].
+ * Pointer axes are accepted on operands (expressions, reductions, copies), not
+ * on results. Strides and offsets are in BYTES; stride 0 broadcasts an axis.
  */
+#define NCA_VIEW_SUBOFFSETS 1
 typedef struct nca_view {
   void* data;
   int32_t dtype;
@@ -94,7 +100,7 @@ typedef struct nca_view {
   int64_t strides[NCA_MAX_NDIM];
   int64_t offsets[NCA_MAX_NDIM];
   int32_t pointer_axis;
-  int32_t flags;            /* reserved, must be 0 */
+  int32_t flags;            /* 0, or NCA_VIEW_SUBOFFSETS with a pointer axis */
 } nca_view;
 
 /*

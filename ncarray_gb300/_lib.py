@@ -125,6 +125,9 @@ def call(name: str, *args) -> None:
     check(getattr(lib(), name)(*args))
 
 
+VIEW_SUBOFFSETS = 1   # nca_view.flags: PEP 3118 suboffset semantics on the pointer axis
+
+
 def make_view(ptr: int, dtype: int, shape, byte_strides, byte_offset: int = 0) -> View:
     v = View()
     v.data = ptr + byte_offset if ptr else None

@@ -78,6 +78,9 @@ class NCDevArray:
         self._buf = _buf
         self._offset = int(_offset)
         self.strides = tuple(int(s) for s in (_strides if _strides is not None else _c_strides(self.shape, isz)))
+        # pointer-axis views (from_panels): axis 0 indexes a device table of
+        # panel pointers; None for ordinary arrays
+        self._ptr = None
 
     # ---- metadata ----
     @property
@@ -104,10 +107,41 @@ class NCDevArray:
         return int(self._buf.data_ptr()) + self._offset
 
     def is_contiguous(self) -> bool:
-        return list(self.strides) == _c_strides(self.shape, self.itemsize)
+        return self._ptr is None and list(self.strides) == _c_strides(self.shape, self.itemsize)
 
     def view_struct(self) -> _lib.View:
-        return _lib.make_view(self.ptr, self.dtype, self.shape, self.strides)
+        v = _lib.make_view(self.ptr, self.dtype, self.shape, self.strides)
+        if self._ptr is not None:
+            v.pointer_axis = 0
+            if self._ptr["step"] == 1:
+                # NC: the view's data is the first table entry; later axes' offsets
+                # land on the panel side
+                if self.ndim > 1:
+                    v.offsets[1] = self._ptr["poff"]
+            else:
+                # a stepped table: SO semantics (stride along the table, suboffset)
+                v.flags = _lib.VIEW_SUBOFFSETS
+                v.offsets[0] = self._ptr["poff"]
+        return v
+
+    @classmethod
+    def from_panels(cls, panels: Sequence["NCDevArray"]) -> "NCDevArray":
+        """An array of shape (len(panels), *panel.shape) whose axis 0 is a
+        pointer axis: element [i, ...] lives in panels[i] (ncarray's NCArray with
+        a pointer axis, src/lib/ncarray/layout.hh:451-535). The panels share
+        shape, dtype and strides; they are kept alive by the result."""
+        panels = list(panels)
+        if not panels:
+            raise ValueError("at least one panel")
+        p0 = panels[0]
+        for p in panels:
+            if p._ptr is not None or p.shape != p0.shape or p.dtype != p0.dtype or p.strides != p0.strides:
+                raise ValueError("panels must be ordinary arrays of one shape, dtype and strides")
+        table = cls.from_host(np.array([p.ptr for p in panels], dtype=np.uint64))
+        out = cls((len(panels),) + p0.shape, p0.dtype, _buf=table._buf, _offset=table._offset,
+                  _strides=(8,) + p0.strides)
+        out._ptr = {"table": table, "panels": panels, "poff": 0, "step": 1}
+        return out
 
     def __len__(self) -> int:
         return self.shape[0]
@@ -182,6 +216,8 @@ class NCDevArray:
 
     # ---- views ----
     def transpose(self, *axes) -> "NCDevArray":
+        if self._ptr is not None:
+            raise NotImplementedError("pointer-axis arrays keep their axis order; copy() them first")
         if len(axes) == 1 and isinstance(axes[0], (tuple, list)):
             axes = tuple(axes[0])
         if not axes:
@@ -194,6 +230,8 @@ class NCDevArray:
     permute = transpose
 
     def reshape(self, *shape) -> "NCDevArray":
+        if self._ptr is not None:
+            raise NotImplementedError("pointer-axis arrays keep their axis order; copy() them first")
         if len(shape) == 1 and isinstance(shape[0], (tuple, list)):
             shape = tuple(shape[0])
         shape = list(shape)
@@ -212,6 +250,8 @@ class NCDevArray:
         return NCDevArray(shape, self.dtype, _buf=src._buf, _offset=src._offset)
 
     def broadcast_to(self, shape: Sequence[int]) -> "NCDevArray":
+        if self._ptr is not None:
+            raise NotImplementedError("pointer-axis arrays keep their axis order; copy() them first")
         shape = tuple(shape)
         pad = len(shape) - self.ndim
         st = [0] * pad + list(self.strides)
@@ -223,9 +263,44 @@ class NCDevArray:
                 raise ValueError("cannot broadcast")
         return NCDevArray(shape, self.dtype, _buf=self._buf, _offset=self._offset, _strides=st)
 
+    def _ptr_getitem(self, key) -> "NCDevArray":
+        """Indexing of a pointer-axis array: an integer on axis 0 selects a
+        panel (an ordinary array); slices on axis 0 select table entries; the
+        other axes slice every panel alike."""
+        key = key + (slice(None),) * (self.ndim - len(key))
+        if len(key) > self.ndim or any(k is None or k is Ellipsis for k in key):
+            raise IndexError("pointer-axis arrays take one index or slice per axis")
+        k0, rest = key[0], key[1:]
+        if not isinstance(k0, slice):
+            i = int(k0)
+            if i < 0:
+                i += self.shape[0]
+            if not 0 <= i < self.shape[0]:
+                raise IndexError("index out of range")
+            panel = self._ptr["panels"][self._ptr.get("first", 0) + i * self._ptr["step"]]
+            inner = NCDevArray(self.shape[1:], self.dtype, _buf=panel._buf,
+                               _offset=panel._offset + self._ptr["poff"], _strides=self.strides[1:])
+            return inner[rest] if rest else inner
+        start, stop, step = k0.indices(self.shape[0])
+        cnt = max(0, (stop - start + (step - (1 if step > 0 else -1))) // step)
+        if step < 0:
+            raise IndexError("negative steps on the pointer axis are not supported")
+        # the inner axes as a probe view (offset 0) to get their shape/strides/offset
+        probe = NCDevArray(self.shape[1:], self.dtype, _buf=self._buf, _offset=0, _strides=self.strides[1:])[rest] \
+            if rest else NCDevArray(self.shape[1:], self.dtype, _buf=self._buf, _offset=0, _strides=self.strides[1:])
+        out = NCDevArray((cnt,) + probe.shape, self.dtype, _buf=self._buf, _offset=self._offset + start * self.strides[0],
+                         _strides=(self.strides[0] * step,) + probe.strides)
+        out._ptr = dict(self._ptr)
+        out._ptr["poff"] = self._ptr["poff"] + probe._offset
+        out._ptr["step"] = self._ptr["step"] * step
+        out._ptr["first"] = self._ptr.get("first", 0) + start * self._ptr["step"]
+        return out
+
     def __getitem__(self, key) -> "NCDevArray":
         if not isinstance(key, tuple):
             key = (key,)
+        if self._ptr is not None:
+            return self._ptr_getitem(key)
         if Ellipsis in key:
             i = key.index(Ellipsis)
             key = key[:i] + (slice(None),) * (self.ndim - len(key) + 1) + key[i + 1:]
@@ -573,6 +648,8 @@ class DevExpr:
 
 
 def _view_key(a: NCDevArray):
+    if a._ptr is not None:
+        return (a.ptr, int(a.dtype), a.shape, a.strides, "ptr", a._ptr["poff"], a._ptr["step"])
     return (a.ptr, int(a.dtype), a.shape, a.strides)
 
 

@@ -166,6 +166,12 @@ struct CArr {
   const char* base = nullptr;
   int dtype = 0;
   int64_t st[NCA_MAX_NDIM] = {0};
+  // operands on a pointer axis: element address = *(table + sum_d c_d pts[d])
+  // + ptc + sum_d c_d st[d] (st holds the panel strides, base is null)
+  bool ptr = false;
+  const char* table = nullptr;
+  int64_t pts[NCA_MAX_NDIM] = {0};
+  int64_t ptc = 0;
 };
 
 struct Space {
@@ -179,11 +185,14 @@ struct Space {
   int64_t total() const { int64_t t = 1; for (int d = 0; d < nd; ++d) t *= shape[d]; return t; }
 };
 
-static void check_view(const nca_view& v, const char* what) {
+static void check_view(const nca_view& v, const char* what, bool pointer_ok = false) {
   if (v.ndim < 0 || v.ndim > NCA_MAX_NDIM) fail(NCA_ERR_LIMIT, "%s: ndim %d (0..%d)", what, v.ndim, NCA_MAX_NDIM);
   if (!dtype_valid(v.dtype)) fail(NCA_ERR_DTYPE, "%s: dtype %d not supported on the device", what, v.dtype);
-  if (v.pointer_axis >= 0) fail(NCA_ERR_UNSUPPORTED, "%s: pointer axes are not supported on the device path", what);
-  if (v.flags != 0) fail(NCA_ERR_INVALID, "%s: flags must be 0", what);
+  if (v.pointer_axis >= 0 && !pointer_ok)
+    fail(NCA_ERR_UNSUPPORTED, "%s: pointer axes are supported on operands, not on results", what);
+  if (v.pointer_axis >= v.ndim) fail(NCA_ERR_INVALID, "%s: pointer axis %d of %d", what, v.pointer_axis, v.ndim);
+  if ((v.flags & ~NCA_VIEW_SUBOFFSETS) != 0 || ((v.flags & NCA_VIEW_SUBOFFSETS) && v.pointer_axis < 0))
+    fail(NCA_ERR_INVALID, "%s: flags %d", what, v.flags);
   int64_t n = 1;
   for (int d = 0; d < v.ndim; ++d) {
     if (v.shape[d] < 0) fail(NCA_ERR_SHAPE, "%s: negative extent", what);
@@ -203,7 +212,28 @@ static Space make_space(const int64_t* lshape, int n, const nca_view* ops, int n
                         const nca_view* out, uint32_t red_mask, const nca_reduction* reds, int nred) {
   Space s;
   for (int k = 0; k < nops; ++k) {
-    CArr a; a.base = view_base(ops[k]); a.dtype = ops[k].dtype; s.ops.push_back(a);
+    CArr a; a.dtype = ops[k].dtype;
+    const nca_view& v = ops[k];
+    if (v.pointer_axis < 0) {
+      a.base = view_base(v);
+    } else {
+      // NC (layout.hh:468-535): axes before the pointer axis move the table
+      // pointer, the pointer axis indexes it (index offset offsets[pa]), later
+      // axes move the panel pointer. SO (suboffsets, layout.hh:677-778): the
+      // pointer axis strides the table and offsets[pa] is added after reading.
+      const int pa = v.pointer_axis;
+      const bool so = (v.flags & NCA_VIEW_SUBOFFSETS) != 0;
+      a.ptr = true;
+      int64_t t = 0, c = 0;
+      for (int d = 0; d < v.ndim; ++d) {
+        if (d < pa) t += v.offsets[d];
+        else if (d == pa) { if (so) c += v.offsets[d]; else t += v.offsets[d] * (int64_t)sizeof(void*); }
+        else c += v.offsets[d];
+      }
+      a.table = static_cast<const char*>(v.data) + t;
+      a.ptc = c;
+    }
+    s.ops.push_back(a);
   }
   if (out) { s.has_out = true; s.out.base = view_base(*out); s.out.dtype = out->dtype; }
   for (int k = 0; k < nred; ++k) {
@@ -221,7 +251,14 @@ static Space make_space(const int64_t* lshape, int n, const nca_view* ops, int n
     for (int k = 0; k < nops; ++k) {
       const nca_view& v = ops[k];
       const int vd = d - (n - v.ndim);
-      s.ops[k].st[c] = (vd >= 0 && v.shape[vd] != 1) ? v.strides[vd] : 0;
+      const bool live = vd >= 0 && v.shape[vd] != 1;
+      if (v.pointer_axis < 0 || vd > v.pointer_axis) {
+        s.ops[k].st[c] = live ? v.strides[vd] : 0;
+      } else {
+        // a table axis: stride of the table (a pointer per index on NC's pointer axis)
+        const bool nc_pa = vd == v.pointer_axis && !(v.flags & NCA_VIEW_SUBOFFSETS);
+        s.ops[k].pts[c] = live ? (nc_pa ? (int64_t)sizeof(void*) : v.strides[vd]) : 0;
+      }
     }
     if (out) s.out.st[c] = out->strides[d];
     for (int k = 0; k < nred; ++k) s.reds[k].st[c] = is_red ? 0 : reds[k].out.strides[kd];
@@ -231,7 +268,9 @@ static Space make_space(const int64_t* lshape, int n, const nca_view* ops, int n
 
 static bool mergeable(const Space& s, int i) {  // dims i (outer) and i+1 (inner)
   if (s.red[i] != s.red[i + 1]) return false;
-  auto ok = [&](const CArr& a) { return a.st[i] == a.st[i + 1] * s.shape[i + 1]; };
+  auto ok = [&](const CArr& a) {
+    return a.st[i] == a.st[i + 1] * s.shape[i + 1] && a.pts[i] == a.pts[i + 1] * s.shape[i + 1];
+  };
   for (auto& a : s.ops) if (!ok(a)) return false;
   if (s.has_out && !ok(s.out)) return false;
   for (auto& a : s.reds) if (!ok(a)) return false;
@@ -244,7 +283,8 @@ static void merge_dims(Space& s) {
     s.shape[i] *= s.shape[i + 1];
     auto fold = [&](CArr& a) {
       a.st[i] = a.st[i + 1];
-      for (int d = i + 1; d + 1 < s.nd; ++d) a.st[d] = a.st[d + 1];
+      a.pts[i] = a.pts[i + 1];
+      for (int d = i + 1; d + 1 < s.nd; ++d) { a.st[d] = a.st[d + 1]; a.pts[d] = a.pts[d + 1]; }
     };
     for (auto& a : s.ops) fold(a);
     if (s.has_out) fold(s.out);
@@ -259,7 +299,10 @@ static void permute_dims(Space& s, const std::vector<int>& perm) {
   for (int c = 0; c < s.nd; ++c) {
     t.shape[c] = s.shape[perm[c]];
     t.red[c] = s.red[perm[c]];
-    for (size_t k = 0; k < s.ops.size(); ++k) t.ops[k].st[c] = s.ops[k].st[perm[c]];
+    for (size_t k = 0; k < s.ops.size(); ++k) {
+      t.ops[k].st[c] = s.ops[k].st[perm[c]];
+      t.ops[k].pts[c] = s.ops[k].pts[perm[c]];
+    }
     if (s.has_out) t.out.st[c] = s.out.st[perm[c]];
     for (size_t k = 0; k < s.reds.size(); ++k) t.reds[k].st[c] = s.reds[k].st[perm[c]];
   }
@@ -299,11 +342,12 @@ struct Spec {
   // loop dim, number of p-row operands, log2(tp / 8)
   int ns = 0, ld = 0, npc = 0, ltp8 = 3, nmaps = 1;
   uint32_t pmask = 0, umask = 0, uumask = 0;
+  uint32_t ptrmask = 0;   // operands on a pointer axis (kinds 2, 3, 4)
 };
 
 struct WordLayout {
   int opb, ops, outb, outs, shape, scal, redb, reds, total, psum, pmax, pmin, nsplit, chunk,
-      keptn, redn, status, aux, magic, nwords;
+      keptn, redn, status, aux, magic, ptb, pts, ptc, nwords;
 };
 
 // symbol of each kernel class (distinct names keep profiler launch lists readable)
@@ -334,6 +378,10 @@ static WordLayout word_layout(int nops, int nd, int nscal, int nred) {
   L.total = p++; L.psum = p++; L.pmax = p++; L.pmin = p++; L.nsplit = p++; L.chunk = p++;
   L.keptn = p++; L.redn = p++; L.status = p++; L.aux = p++;
   L.magic = p; p += nd;
+  // pointer-axis tables (every operand has a slot; used by NCA_PTRMASK operands)
+  L.ptb = p; p += nops;
+  L.pts = p; p += nops * nd;
+  L.ptc = p; p += nops;
   L.nwords = p;
   return L;
 }
@@ -503,7 +551,8 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_W_PSUM " << L.psum << "\n#define NCA_W_PMAX " << L.pmax << "\n#define NCA_W_PMIN " << L.pmin
      << "\n#define NCA_W_NSPLIT " << L.nsplit << "\n#define NCA_W_CHUNK " << L.chunk << "\n#define NCA_W_KEPTN " << L.keptn
      << "\n#define NCA_W_REDN " << L.redn << "\n#define NCA_W_STATUS " << L.status << "\n#define NCA_W_AUX " << L.aux
-     << "\n#define NCA_W_MAGIC " << L.magic
+     << "\n#define NCA_W_MAGIC " << L.magic << "\n#define NCA_W_PTB " << L.ptb << "\n#define NCA_W_PTS " << L.pts
+     << "\n#define NCA_W_PTC " << L.ptc << "\n#define NCA_PTRMASK " << sp.ptrmask << "u"
      << "\n";
   os << "#define NCA_NS " << sp.ns << "\n#define NCA_LD " << sp.ld << "\n#define NCA_NPC " << sp.npc << "\n#define NCA_LTP8 "
      << sp.ltp8 << "\n#define NCA_PMASK " << sp.pmask << "u\n#define NCA_UMASK " << sp.umask << "u\n#define NCA_UUMASK " << sp.uumask << "u\n#define NCA_NMAPS "
@@ -822,7 +871,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.kept_mask); add(sp.has_out); add(sp.out_dtype); add(sp.w); add(sp.r); add(sp.nred); add(sp.red_ops);
   add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
-  add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask);
+  add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
   for (int d : sp.op_dtypes) add(d);
   k += '|';
   for (int m : sp.op_modes) add(m);
@@ -883,11 +932,14 @@ static void plan_vec(const Space& s, Spec& sp, int max_vec_elems, bool with_out)
     return true;
   };
   while (vec > 1 && (s.shape[ax] % vec != 0 || !out_ok(vec))) vec >>= 1;
+  // a table axis innermost: every lane reads its own panel pointer
+  for (int k = 0; k < sp.nops; ++k) if (s.ops[k].ptr && s.ops[k].pts[ax] != 0) vec = 1;
   sp.vec = vec;
   sp.op_modes.assign(sp.nops, M_STRIDED);
   for (int k = 0; k < sp.nops; ++k) {
     const CArr& a = s.ops[k];
     const int64_t isz = dtinfo(a.dtype).size;
+    if (a.ptr) { sp.op_modes[k] = a.st[ax] == 0 && a.pts[ax] == 0 ? M_CONST : M_STRIDED; continue; }
     if (a.st[ax] == 0) { sp.op_modes[k] = M_CONST; continue; }
     if (vec == 1) { sp.op_modes[k] = M_STRIDED; continue; }
     bool ok = a.st[ax] == isz && aligned(a.base, vec * isz);
@@ -929,6 +981,13 @@ static void fill_common_words(const Space& s, const Spec& sp, const Tape& t, con
   }
   w[L.total] = (uint64_t)s.total();
   w[L.status] = (uint64_t)(uintptr_t)jit_status_word();
+  for (int k = 0; k < sp.nops; ++k) {
+    if (!s.ops[k].ptr) continue;
+    w[L.opb + k] = 0;   // the kernel adds the panel address itself
+    w[L.ptb + k] = (uint64_t)(uintptr_t)s.ops[k].table;
+    for (int d = 0; d < sp.nd; ++d) w[L.pts + k * sp.nd + d] = (uint64_t)s.ops[k].pts[d];
+    w[L.ptc + k] = (uint64_t)s.ops[k].ptc;
+  }
 }
 
 static void launch(CUfunction fn, int64_t grid, std::vector<uint64_t>& words, cudaStream_t stream,
@@ -1255,7 +1314,7 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
   check_view(out, "out");
   if (nops < 0 || nops > NCA_MAX_OPERANDS) fail(NCA_ERR_LIMIT, "%d operands (0..%d)", nops, NCA_MAX_OPERANDS);
   if (tape.n_arrays > nops) fail(NCA_ERR_INVALID, "tape loads more operands than given");
-  for (int k = 0; k < nops; ++k) { check_view(ops[k], "operand"); check_broadcast(out.shape, out.ndim, ops[k], "operand"); }
+  for (int k = 0; k < nops; ++k) { check_view(ops[k], "operand", true); check_broadcast(out.shape, out.ndim, ops[k], "operand"); }
   int64_t n = 1;
   for (int d = 0; d < out.ndim; ++d) n *= out.shape[d];
   if (n == 0) return;
@@ -1274,9 +1333,10 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
   sp.nops = nops; sp.nd = s.nd; sp.has_out = true; sp.out_dtype = out.dtype; sp.w = tape.compute_dtype;
   sp.r = tape.result_dtype; sp.nscal = (int)tape.scalar_dtypes.size();
   for (int k = 0; k < nops; ++k) sp.op_dtypes.push_back(ops[k].dtype);
+  for (int k = 0; k < nops; ++k) if (s.ops[k].ptr) sp.ptrmask |= 1u << k;
   // transposed operands: stage them (kind 6) with p and q kept and every other
   // dim walked as a loop dim; the output must be contiguous along p
-  if (!tape.uses_idx && s.nd >= 2 && s.out.st[s.nd - 1] == dtinfo(out.dtype).size) {
+  if (!tape.uses_idx && sp.ptrmask == 0 && s.nd >= 2 && s.out.st[s.nd - 1] == dtinfo(out.dtype).size) {
     uint32_t tmask = 0;
     int nt = 0;
     const int qd = find_staged(s, tmask, nt);
@@ -1291,7 +1351,7 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
       return;
     }
   }
-  bool flat = s.nd == 1 && s.out.st[0] == dtinfo(out.dtype).size;
+  bool flat = s.nd == 1 && s.out.st[0] == dtinfo(out.dtype).size && sp.ptrmask == 0;
   for (int k = 0; k < nops && flat; ++k)
     if (s.ops[k].st[0] != 0 && s.ops[k].st[0] != dtinfo(ops[k].dtype).size) flat = false;
   plan_vec(s, sp, 16, true);
@@ -1335,7 +1395,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   if (nred < 1 || nred > NCA_MAX_REDUCTIONS) fail(NCA_ERR_LIMIT, "%d reductions (1..%d)", nred, NCA_MAX_REDUCTIONS);
   if (nops < 0 || nops > NCA_MAX_OPERANDS) fail(NCA_ERR_LIMIT, "%d operands (0..%d)", nops, NCA_MAX_OPERANDS);
   if (tape.n_arrays > nops) fail(NCA_ERR_INVALID, "tape loads more operands than given");
-  for (int k = 0; k < nops; ++k) check_view(ops[k], "operand");
+  for (int k = 0; k < nops; ++k) check_view(ops[k], "operand", true);
   int64_t lshape[NCA_MAX_NDIM];
   int n;
   if (out) {
@@ -1387,6 +1447,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   sp.r = tape.result_dtype; sp.nscal = (int)tape.scalar_dtypes.size(); sp.nred = nred; sp.red_ops = red_ops;
   sp.has_sum = has_sum; sp.has_max = has_max; sp.has_min = has_min;
   for (int k = 0; k < nops; ++k) sp.op_dtypes.push_back(ops[k].dtype);
+  for (int k = 0; k < nops; ++k) if (s.ops[k].ptr) sp.ptrmask |= 1u << k;
   merge_dims(s);
   ensure_nd1(s);
   const bool inner_reduced = (RN == 0) || s.red[s.nd - 1];
@@ -1449,7 +1510,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   {
     uint32_t tmask = 0;
     int nt = 0;
-    const int qd = tape.uses_idx ? -1 : find_staged(s, tmask, nt);
+    const int qd = (tape.uses_idx || sp.ptrmask != 0) ? -1 : find_staged(s, tmask, nt);
     if (qd >= 0) {
       launch_staged(s, sp, tape, qd, tmask, nt, KN, RN, stream);
       return;
@@ -1528,6 +1589,22 @@ int jit_selftest(const char* arch) {
       const std::string src = gen_source(sp, t);
       nvrtc_compile(src, a);
       ++n;
+    }
+    // kinds 2, 3, 4 with operand 0 on a pointer axis (first two dtype rows)
+    if (&d - &dts[0] < 2) {
+      for (int kind = 2; kind <= 4; ++kind) {
+        Spec sp;
+        sp.kind = kind; sp.nops = 3; sp.nd = 3; sp.vec = 1; sp.idx32 = 1; sp.w = d[0]; sp.r = d[1]; sp.out_dtype = d[1];
+        sp.nscal = 1; sp.op_dtypes = {d[2], d[2], d[2]}; sp.op_modes = {M_STRIDED, M_CONST, M_STRIDED};
+        sp.ptrmask = 1u;
+        sp.has_out = kind != 3;
+        if (kind >= 3) {
+          sp.nred = 2; sp.red_ops = 0u | (4u << 4); sp.has_sum = sp.has_max = true;
+          if (kind == 3) { sp.nkept = 1; sp.kept_mask = 1u; } else sp.kept_mask = 1u | 4u;
+        }
+        nvrtc_compile(gen_source(sp, t), a);
+        ++n;
+      }
     }
     // kind 6: operand 0 staged through shared memory, dims (q, b, r, p)
     Spec sp;

@@ -36,7 +36,7 @@ def test_version_and_stats(built_lib):
 def test_nvrtc_compiles_every_kernel_class(built_lib):
     n = ctypes.c_int32(0)
     _lib.call("nca_jit_selftest", b"sm_103a", ctypes.byref(n))
-    assert n.value == 48
+    assert n.value == 54
 
 
 def _tape(instrs, cdt=DType.float32, rdt=DType.float32):
@@ -88,10 +88,19 @@ def test_bad_views_rejected(built_lib):
     bad = _view([5])
     ops = (_lib.View * 1)(bad)
     assert L.nca_expr_eval(ctypes.byref(t), ops, 1, ctypes.byref(out), None) == _lib.ERR_SHAPE
-    ptr = _view([4])
-    ptr.pointer_axis = 0
-    ops = (_lib.View * 1)(ptr)
-    assert L.nca_expr_eval(ctypes.byref(t), ops, 1, ctypes.byref(out), None) == _lib.ERR_UNSUPPORTED
+    # pointer axes: accepted on operands, rejected on results, checked for range and flags
+    good = (_lib.View * 1)(_view([4]))
+    pout = _view([4])
+    pout.pointer_axis = 0
+    assert L.nca_expr_eval(ctypes.byref(t), good, 1, ctypes.byref(pout), None) == _lib.ERR_UNSUPPORTED
+    prange = _view([4])
+    prange.pointer_axis = 1
+    ops = (_lib.View * 1)(prange)
+    assert L.nca_expr_eval(ctypes.byref(t), ops, 1, ctypes.byref(out), None) == _lib.ERR_INVALID
+    pflags = _view([4])
+    pflags.flags = 1          # suboffset semantics without a pointer axis
+    ops = (_lib.View * 1)(pflags)
+    assert L.nca_expr_eval(ctypes.byref(t), ops, 1, ctypes.byref(out), None) == _lib.ERR_INVALID
     cplx = _view([4], DType.float32)
     cplx.dtype = 13
     ops = (_lib.View * 1)(cplx)
