@@ -356,6 +356,73 @@ def measure_c4(torch, nca, peak, reps=5):
     return out
 
 
+def measure_binning(torch, nca, peak, flush_buf, reps=20):
+    """Pixel binning, the reference's own benchmark (examples/benchmark_binning.cu):
+    a (32, 512, 1024) float32 image binned 2 x 2 x 2 into (16, 256, 512) as the
+    fused sum of 8 strided views times 1/8, on contiguous data and on a
+    32-panel pointer-axis view, and as reshape(16,2,256,2,512,2).sum((1,3,5)).
+    64 MB read + 8 MB written per call; L2 flushed before every call (the image
+    fits in L2); eager calls and CUDA-graph replays."""
+    shape, bins = (32, 512, 1024), (2, 2, 2)
+    g = torch.Generator(device="cuda").manual_seed(SEED + 7)
+    data = nca.NCDevArray(shape, nca.DType.float32)
+    data._buf.view(torch.float32).copy_(torch.rand(32 * 512 * 1024, generator=g, device="cuda"))
+    panels = [data[i].copy() for i in range(32)]
+    P = nca.NCDevArray.from_panels(panels)
+
+    def fused(src):
+        e = None
+        with nca.lazy_mode():
+            for a in range(2):
+                for b in range(2):
+                    for c in range(2):
+                        v = src[a::2, b::2, c::2]
+                        e = v if e is None else e + v
+            return e * 0.125
+
+    e_c, e_p = fused(data), fused(P)
+    out = nca.NCDevArray((16, 256, 512), nca.DType.float32)
+    six = data.reshape(16, 2, 256, 2, 512, 2)._expr()
+    bytes_per = 32 * 512 * 1024 * 4 + 16 * 256 * 512 * 4
+    forms = {"fused_views": lambda: e_c.evaluate(out=out),
+             "fused_views_panels": lambda: e_p.evaluate(out=out),
+             "reshape_sum": lambda: six.evaluate(reductions=[(nca.RedOp.SUM, (1, 3, 5))], red_out=[out])}
+    s = torch.cuda.current_stream()
+    res = {}
+    for name, fn in forms.items():
+        fn()
+        fn()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            fn()
+        for mode, call in (("eager", fn), ("graph", graph.replay)):
+            call()
+            tot = 0.0
+            for _ in range(reps):
+                flush_buf.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                call()
+                e1.record(s)
+                torch.cuda.synchronize()
+                tot += e0.elapsed_time(e1)
+            ms = tot / reps
+            gbs = bytes_per / (ms * 1e-3) / 1e9
+            res[f"{name}_{mode}"] = {"GB/s": round(gbs, 1), "frac_of_measured": round(gbs / peak, 4),
+                                     "us": round(ms * 1e3, 2)}
+    # all forms agree (sums of eight values: the reduction may round differently)
+    e_c.evaluate(out=out)
+    a = out.to_host().copy()
+    e_p.evaluate(out=out)
+    b = out.to_host().copy()
+    six.evaluate(reductions=[(nca.RedOp.SUM, (1, 3, 5))], red_out=[out])
+    c = out.to_host() * np.float32(0.125)
+    res["panels_bit_exact_vs_contiguous"] = bool(np.array_equal(a, b))
+    res["reshape_sum_max_rel_diff"] = float(np.max(np.abs(c - a) / np.maximum(np.abs(a), 1e-30)))
+    res["l2"] = "flushed before every call"
+    return res
+
+
 def c5_arrays(torch, nca, n_arrays):
     """n_arrays 1-D device arrays with lengths log-uniform in [64, 2^22],
     alternately float32 and bfloat16, x = exp(N(0, 2)) with random signs,
@@ -537,7 +604,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--headline-only", action="store_true", help="skip the per-op measurements of the other workloads")
-    ap.add_argument("--only", default=None, choices=["c1", "c3", "c4", "c5"],
+    ap.add_argument("--only", default=None, choices=["c1", "c3", "c4", "c5", "binning"],
                     help="measure one per-op workload and print its figures (no headline line)")
     ap.add_argument("--profile-op", default=None, help="run one op --steps times for a profiler capture")
     args = ap.parse_args()
@@ -553,9 +620,10 @@ def main():
         import torch
         import ncarray_gb300 as nca
         peak, _ = peaks()
-        flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device="cuda") if args.only == "c1" else None
+        flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device="cuda") if args.only in ("c1", "binning") else None
         fn = {"c1": lambda: measure_c1(torch, nca, peak, flush_buf), "c3": lambda: measure_c3(torch, nca, peak),
-              "c4": lambda: measure_c4(torch, nca, peak), "c5": lambda: measure_c5(torch, nca, peak)}[args.only]
+              "c4": lambda: measure_c4(torch, nca, peak), "c5": lambda: measure_c5(torch, nca, peak),
+              "binning": lambda: measure_binning(torch, nca, peak, flush_buf)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
         return
 
@@ -766,7 +834,8 @@ def main():
         for name, fn in (("c1_fused_f64", lambda: measure_c1(torch, nca, peak, flush_buf)),
                          ("c3_stencil_f32", lambda: measure_c3(torch, nca, peak)),
                          ("c4_hist2d", lambda: measure_c4(torch, nca, peak)),
-                         ("c5_batched", lambda: measure_c5(torch, nca, peak))):
+                         ("c5_batched", lambda: measure_c5(torch, nca, peak)),
+                         ("binning", lambda: measure_binning(torch, nca, peak, flush_buf))):
             try:
                 per_op[name] = fn()
             except Exception as ex:  # a failed side measurement must not hide the headline

@@ -24,7 +24,7 @@ extern "C" {
 #endif
 
 #define NCA_MAX_NDIM 10   /* NCARRAY_MAX_NDIM, src/lib/ncarray/custom_types.hh:65-67 */
-#define NCA_MAX_OPERANDS 24
+#define NCA_MAX_OPERANDS 64
 #define NCA_MAX_SCALARS 32
 #define NCA_MAX_INSTRS 128
 #define NCA_MAX_REDUCTIONS 4

@@ -364,7 +364,7 @@ static const char* kernel_name(int kind) {
   return "nca_kernel";
 }
 
-static WordLayout word_layout(int nops, int nd, int nscal, int nred) {
+static WordLayout word_layout(int nops, int nd, int nscal, int nred, bool ptr) {
   WordLayout L;
   int p = 0;
   L.opb = p; p += nops;
@@ -378,10 +378,10 @@ static WordLayout word_layout(int nops, int nd, int nscal, int nred) {
   L.total = p++; L.psum = p++; L.pmax = p++; L.pmin = p++; L.nsplit = p++; L.chunk = p++;
   L.keptn = p++; L.redn = p++; L.status = p++; L.aux = p++;
   L.magic = p; p += nd;
-  // pointer-axis tables (every operand has a slot; used by NCA_PTRMASK operands)
-  L.ptb = p; p += nops;
-  L.pts = p; p += nops * nd;
-  L.ptc = p; p += nops;
+  // pointer-axis tables (a slot per operand when a launch has pointer operands)
+  L.ptb = p; p += ptr ? nops : 0;
+  L.pts = p; p += ptr ? nops * nd : 0;
+  L.ptc = p; p += ptr ? nops : 0;
   L.nwords = p;
   return L;
 }
@@ -521,7 +521,7 @@ static std::string lim_expr(int dt, bool lowest) {
 }
 
 static std::string gen_source(const Spec& sp, const Tape& t) {
-  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
   std::ostringstream os;
   os << kPrelude;
   os << "#define NCA_NOPS " << sp.nops << "\n#define NCA_ND " << sp.nd << "\n#define NCA_NRED " << sp.nred
@@ -1186,7 +1186,7 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   if (per_sm < 1) return false;
   const int64_t U = KN / ((int64_t)tp * QX), NB = RN / rb, W = U * NB;
   const int64_t G = std::min<int64_t>((int64_t)sms * per_sm, W);
-  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
   std::vector<uint64_t> w;
   fill_common_words(s, sp, tape, L, w);
   w[L.nsplit] = (uint64_t)G; w[L.chunk] = 0; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
@@ -1288,7 +1288,7 @@ static void launch_staged(const Space& s, Spec sp, const Tape& tape, int qd, uin
   int64_t C = RN > 0 ? cdiv(cdiv(RN, S), sp.rb) * sp.rb : 0;
   if (C > 0) S = cdiv(RN, C);
   if (S < 1) S = 1;
-  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
   std::vector<uint64_t> w;
   fill_common_words(s, sp, tape, L, w);
   w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
@@ -1364,7 +1364,7 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
   bool small_dims = true;
   for (int d = 0; d < s.nd; ++d) if (s.shape[d] >= (1ll << 31)) small_dims = false;
   sp.idx32 = (total / sp.vec < (1ll << 31) && small_dims) ? 1 : 0;
-  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, 0);
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, 0, sp.ptrmask != 0);
   std::vector<uint64_t> w;
   fill_common_words(s, sp, tape, L, w);
   for (int d = 0; d < s.nd; ++d) {
@@ -1472,7 +1472,9 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
     if (RN > 0) plan_vec(s, sp, 16, false); else { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
     if (sp.vec > 1 && s.shape[s.nd - 1] % sp.vec != 0) { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
-    sp.team = RN >= 4096 ? 256 : 32;
+    // team of threads per kept position: a block for long reductions, a warp
+    // for medium ones, one thread when fewer than 64 elements are reduced
+    sp.team = RN >= 4096 ? 256 : (RN >= 64 ? 32 : 1);
     const int64_t tpb = 256 / sp.team;
     const int64_t target = (int64_t)sms * tpb * 4;
     int64_t S = 1;
@@ -1484,7 +1486,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     C = cdiv(C, sp.vec) * sp.vec;
     if (C > 0) S = cdiv(RN, C);
     if (S < 1) S = 1;
-    const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+    const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
     std::vector<uint64_t> w;
     fill_common_words(s, sp, tape, L, w);
     w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
@@ -1526,7 +1528,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   if (KG < target) S = std::min<int64_t>(cdiv(target, KG), std::max<int64_t>(1, RN / 8));
   int64_t C = cdiv(RN, S);
   S = cdiv(RN, C);
-  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred);
+  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
   std::vector<uint64_t> w;
   fill_common_words(s, sp, tape, L, w);
   w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
@@ -1598,6 +1600,7 @@ int jit_selftest(const char* arch) {
         sp.nscal = 1; sp.op_dtypes = {d[2], d[2], d[2]}; sp.op_modes = {M_STRIDED, M_CONST, M_STRIDED};
         sp.ptrmask = 1u;
         sp.has_out = kind != 3;
+        if (kind == 3) sp.team = 1;   // one thread per kept position
         if (kind >= 3) {
           sp.nred = 2; sp.red_ops = 0u | (4u << 4); sp.has_sum = sp.has_max = true;
           if (kind == 3) { sp.nkept = 1; sp.kept_mask = 1u; } else sp.kept_mask = 1u | 4u;
