@@ -740,6 +740,16 @@ def absolute(x):
     return _as_node(x)._unary(OpCode.ABS)
 
 
+def inc(x):
+    """x + 1 in x's dtype (ncarray's INC opcode)."""
+    return _as_node(x)._unary(OpCode.INC)
+
+
+def dec(x):
+    """x - 1 in x's dtype (ncarray's DEC opcode)."""
+    return _as_node(x)._unary(OpCode.DEC)
+
+
 def logical_and(a, b):
     return _as_node(a)._binary(OpCode.LAND, b)
 

@@ -161,6 +161,10 @@ LOAD_AS(i64) LOAD_AS(u64) LOAD_AS(f32) LOAD_AS(f64)
     return (T)(a / b);                                                                      \
   }                                                                                         \
   static T mod_##T(T a, T b);                                                               \
+  static T bnot_##T(T a);                                                                   \
+  static T band_##T(T a, T b);                                                              \
+  static T bor_##T(T a, T b);                                                               \
+  static T xor_##T(T a, T b);                                                               \
   static T abs_##T(T a) {                                                                   \
     if (KIND == 3) return (T)fabsf((float)a);                                               \
     if (KIND == 4) return (T)fabs((double)a);                                               \
@@ -189,6 +193,7 @@ LOAD_AS(i64) LOAD_AS(u64) LOAD_AS(f32) LOAD_AS(f64)
         case OP_INC: st[top] = add_##T(st[top], (T)1); break;                               \
         case OP_DEC: st[top] = sub_##T(st[top], (T)1); break;                               \
         case OP_LNOT: st[top] = (T)(!st[top]); break;                                       \
+        case OP_BNOT: st[top] = bnot_##T(st[top]); break;                                   \
         case OP_ABS: st[top] = abs_##T(st[top]); break;                                     \
         case OP_SQRT: st[top] = sqrt_##T(st[top]); break;                                   \
         default:                                                                            \
@@ -207,6 +212,9 @@ LOAD_AS(i64) LOAD_AS(u64) LOAD_AS(f32) LOAD_AS(f64)
             case OP_GE: st[++top] = (T)(a >= b); break;                                     \
             case OP_LAND: st[++top] = (T)(a && b); break;                                   \
             case OP_LOR: st[++top] = (T)(a || b); break;                                    \
+            case OP_BAND: st[++top] = band_##T(a, b); break;                                \
+            case OP_BOR: st[++top] = bor_##T(a, b); break;                                  \
+            case OP_XOR: st[++top] = xor_##T(a, b); break;                                  \
             default: return -1;                                                             \
           }                                                                                 \
       }                                                                                     \
@@ -214,6 +222,28 @@ LOAD_AS(i64) LOAD_AS(u64) LOAD_AS(f32) LOAD_AS(f64)
     *out = st[0];                                                                           \
     return 0;                                                                               \
   }
+
+/* bitwise ops: the reference VM skips them (dynamicmvnode.hh:238); defined
+ * here as two's complement operations in the compute type, bool NOT as !a
+ * (the device prelude's nca_bnot/band/bor/xor). Floating compute types are
+ * rejected before evaluation. */
+#define BIT_INT(T, U)                                                                         \
+  static T bnot_##T(T a) { return (T)(U)(~(U)a); }                                          \
+  static T band_##T(T a, T b) { return (T)(U)((U)a & (U)b); }                               \
+  static T bor_##T(T a, T b) { return (T)(U)((U)a | (U)b); }                                \
+  static T xor_##T(T a, T b) { return (T)(U)((U)a ^ (U)b); }
+BIT_INT(i8, u8) BIT_INT(u8, u8) BIT_INT(i16, u16) BIT_INT(u16, u16) BIT_INT(i32, u32) BIT_INT(u32, u32)
+BIT_INT(i64, u64) BIT_INT(u64, u64)
+static b8 bnot_b8(b8 a) { return !a; }
+static b8 band_b8(b8 a, b8 b) { return a && b; }
+static b8 bor_b8(b8 a, b8 b) { return a || b; }
+static b8 xor_b8(b8 a, b8 b) { return a != b; }
+#define BIT_FLT(T)                                                                            \
+  static T bnot_##T(T a) { (void)a; return (T)0; }                                          \
+  static T band_##T(T a, T b) { (void)a; (void)b; return (T)0; }                            \
+  static T bor_##T(T a, T b) { (void)a; (void)b; return (T)0; }                             \
+  static T xor_##T(T a, T b) { (void)a; (void)b; return (T)0; }
+BIT_FLT(f32) BIT_FLT(f64)
 
 static b8 mod_b8(b8 a, b8 b) { (void)a; (void)b; return false; }
 #define INT_MOD(T, SIGNED)                                                                  \
@@ -232,8 +262,9 @@ VM_TYPE(i8, u8, 1) VM_TYPE(i16, u16, 1) VM_TYPE(i32, u32, 1) VM_TYPE(i64, u64, 1
 VM_TYPE(u8, u8, 2) VM_TYPE(u16, u16, 2) VM_TYPE(u32, u32, 2) VM_TYPE(u64, u64, 2)
 VM_TYPE(f32, f32, 3) VM_TYPE(f64, f64, 4)
 
-/* bitwise ops the reference VM skips; the device defines them for integer W */
-static int bitwise_ok(const uint32_t* ins, int n) {
+/* bitwise ops are defined for integer and bool compute types only */
+static int bitwise_ok(const uint32_t* ins, int n, int compute_dtype) {
+  if (compute_dtype != D_F32 && compute_dtype != D_F64) return 1;
   for (int i = 0; i < n; ++i) {
     const int op = (int)(ins[i] >> 24);
     if (op == OP_BNOT || op == OP_BAND || op == OP_BOR || op == OP_XOR) return 0;
@@ -288,7 +319,7 @@ int orc_expr_eval(const uint32_t* instrs, int n_instrs, const int* scalar_dtypes
   int dts[32];
   for (int k = 0; k < nops; ++k) dts[k] = ops[k].dtype;
   char* ob = vbase(out);
-  if (!bitwise_ok(instrs, n_instrs)) return 4;
+  if (!bitwise_ok(instrs, n_instrs, compute_dtype)) return 4;
   for (int i = 0; i < n_instrs; ++i) {
     const int op = (int)(instrs[i] >> 24), ix = (int)(instrs[i] & 0xffffff);
     if ((op == OP_LOAD_NCARR || op == OP_LOAD_SOARR) && ix >= nops) return 5;

@@ -167,3 +167,27 @@ def test_empty_and_zero_division(cuda, orc):
     with nca.lazy_mode():
         e = dev(i) % dev(np.array([0, -1, 3, 2], dtype=np.int32))
     check(orc, e, [i, np.array([0, -1, 3, 2], dtype=np.int32)], "int mod edge")
+
+
+@pytest.mark.parametrize("dt", [DType.int32, DType.uint8, DType.int64, DType.float32])
+def test_opcode_matrix(cuda, orc, dt):
+    """Every opcode the device evaluates, alone and mixed with IDX, vs the oracle
+    (bit-exact): comparisons, logical and bitwise ops, INC/DEC/NEG, BNOT."""
+    rng = np.random.default_rng(SEED + 40 + int(dt))
+    shape = (5, 17, 9)
+    a, b = rand(rng, shape, dt), rand(rng, shape, dt)
+    da, db = dev(a, dt), dev(b, dt)
+    with nca.lazy_mode():
+        exprs = {
+            "ne": da != db, "lt": da < db, "le": da <= db, "ge": da >= db,
+            "lor": nca.logical_or(da, db), "lnot": nca.logical_not(da),
+            "inc": nca.inc(da), "dec": nca.dec(da), "neg_inc": -nca.inc(db),
+            "cmp_chain": nca.logical_and(da < db, db != 0),
+            "idx_mix": da + nca.iota(shape, dt),
+        }
+        if dt != DType.float32:
+            exprs.update({"band": da & db, "bor": da | db, "xor": da ^ db, "bnot": ~da,
+                          "bit_chain": (da & 7) | (db ^ 3)})
+    host = {id(da): a, id(db): b}
+    for name, e in exprs.items():
+        check(orc, e, [host[id(x)] for x in e.arrays], f"{dt.name} {name}")

@@ -145,3 +145,17 @@ def test_hist_oracle_small(orc):
     c = counts.reshape(4, 4)
     assert c[0, 0] == 1 and c[2, 2] == 1 and c[3, 3] == 1 and c[3, 1] == 1 and c.sum() == 4
     assert ws.reshape(4, 4)[3, 1] == 6.0
+
+
+def test_oracle_bitwise_ops_match_numpy(orc):
+    """BAND/BOR/XOR/BNOT (which the reference VM skips) are defined as two's
+    complement operations in the compute type; the oracle agrees with numpy."""
+    rng = np.random.default_rng(7)
+    a = rng.integers(-2**31, 2**31, size=257, dtype=np.int64).astype(np.int32)
+    b = rng.integers(-2**31, 2**31, size=257, dtype=np.int64).astype(np.int32)
+    L = lambda i: (2 << 24) | i  # noqa: E731  LOAD_NCARR i
+    for op, want in ((28, a & b), (29, a | b), (30, a ^ b)):
+        got = orc.expr_eval([L(0), L(1), op << 24], [], 8, [(a, 8), (b, 8)], a.shape, 8)
+        assert np.array_equal(got, want), op
+    got = orc.expr_eval([L(0), 13 << 24], [], 8, [(a, 8)], a.shape, 8)
+    assert np.array_equal(got, ~a)
