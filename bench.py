@@ -532,6 +532,20 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
         counts = nca.NCDevArray((1024, 1024), nca.DType.uint64).fill(0)
         wsum = nca.NCDevArray((1024, 1024), nca.DType.float32).fill(0.0)
         fn = lambda: hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0), w, wsum)  # noqa: E731
+    elif op == "binning":
+        # the fused sum of eight strided views of a (32, 512, 1024) image (2x2x2 bins)
+        data = nca.NCDevArray((32, 512, 1024), nca.DType.float32)
+        data._buf.view(torch.float32).copy_(torch.rand(32 * 512 * 1024, device="cuda"))
+        e = None
+        with nca.lazy_mode():
+            for a in range(2):
+                for b in range(2):
+                    for c in range(2):
+                        v = data[a::2, b::2, c::2]
+                        e = v if e is None else e + v
+            e = e * 0.125
+        out = nca.NCDevArray((16, 256, 512), nca.DType.float32)
+        fn = lambda: e.evaluate(out=out)  # noqa: E731
     elif op == "c5-small":
         # the batched reduction on 1,000 of the uneven arrays (about 1 GB)
         from ncarray_gb300.batch import Batch
