@@ -39,7 +39,7 @@ typedef enum nca_status {
   NCA_ERR_CUDA = 5,         /* a CUDA runtime/driver call failed                 */
   NCA_ERR_OOM = 6,          /* device scratch allocation failed                  */
   NCA_ERR_TIMEOUT = 7,      /* a bounded device wait gave up (status word set)   */
-  NCA_ERR_UNSUPPORTED = 8,  /* valid request this build does not implement       */
+  NCA_ERR_UNSUPPORTED = 8,  /* valid request the library does not implement     */
   NCA_ERR_LIMIT = 9         /* a size limit of this ABI was exceeded             */
 } nca_status;
 

@@ -2,7 +2,7 @@
 //
 // The reference has only an internal scatter-add (`dest[idx[i]] += src[i]`,
 // src/lib/ncarray/device/kernels.cuh:660-680, host/elementwise.hh:482-505) and
-// no public histogram API; this is the histogram the benchmark spec asks for.
+// no public histogram API; this file adds one.
 // Binning rule (the oracle restates it bit for bit): in float32,
 //   fx = floor((x - x_lo) * sx),  sx = (float)(nbx / (x_hi - x_lo))   (same for y)
 // and the point is kept only if 0 <= fx < nbx and 0 <= fy < nby (NaN dropped).

@@ -1,11 +1,11 @@
-"""Python access to the parity checkers (TEST INFRASTRUCTURE ONLY).
+"""Python access to the oracle (TEST INFRASTRUCTURE ONLY).
 
 ``liboracle.so``  -- the C restatement of the reference algorithms (oracle.c).
 ``libncref.so``   -- ncarray's own host code compiled from its sources
                      (oracle/_ref, built only where the reference is present).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
-package, and only as the checker (never as the thing measured or shipped).
+package, and only as the oracle (never as the thing measured or shipped).
 """
 from __future__ import annotations
 

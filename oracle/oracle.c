@@ -1,7 +1,7 @@
 /*
  * oracle.c -- CPU restatement of the reference algorithms on the hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker that the GPU kernels are
+ * TEST INFRASTRUCTURE ONLY. This file is the oracle the GPU kernels are
  * compared against; it is never part of the product path. Only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it.
  *

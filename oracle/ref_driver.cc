@@ -32,13 +32,13 @@ using NCArray = ArrayImpl<NCOffsetsPolicy, OwnerPolicy>;
 namespace ncarray {
 namespace host {
 RuntimeCompiler& RuntimeCompiler::instance() {
-  throw std::runtime_error("asmjit host JIT is not available in this build");
+  throw std::runtime_error("asmjit host JIT is not vendored with the reference sources");
 }
 ExprKernelFunc RuntimeCompiler::get_expr_kernel(DType, DType, DType, const SOArrayPolicy&,
                                                 const std::vector<Instruction>&,
                                                 const std::vector<SOArrayPolicy>&,
                                                 const std::vector<Scalar>&, bool) {
-  throw std::runtime_error("asmjit host JIT is not available in this build");
+  throw std::runtime_error("asmjit host JIT is not vendored with the reference sources");
 }
 }  // namespace host
 }  // namespace ncarray
