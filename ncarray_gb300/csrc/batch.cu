@@ -8,14 +8,14 @@
 //   - nca_batch_create splits every array into chunks of `chunk_bytes` and
 //     uploads a descriptor table (array, first element, element count) once;
 //   - the persistent kernel's CTAs walk the chunk table with a static stride
-//     (chunks carry equal bytes, so the walk is balanced), streaming each
-//     chunk through shared memory by bulk copies; each CTA reduces its chunk
-//     with per-thread float-float sums (Knuth TwoSum, packed float32x2) of x
-//     and of fma(x, x, -x), a float max, and a float64 block tree, then
-//     writes one partial record;
-//   - the CTA finishing the last chunk of an array (a per-array counter
-//     incremented after a release fence) combines that array's partials in
-//     chunk order (deterministic) and resets the counter for the next launch.
+//     (chunks carry equal bytes, so the walk is balanced); a producer warp
+//     streams each chunk through shared-memory slabs by bulk copies and the
+//     consumer warps reduce it with per-thread float-float sums (Knuth TwoSum,
+//     packed float32x2) of x and of fma(x, x, -x) and a float max, then a
+//     float-float warp tree; each warp writes one partial record per chunk;
+//   - the warp writing an array's last partial (a per-array counter
+//     incremented after a release fence) combines that array's partials in a
+//     fixed order (deterministic) and resets the counter for the next launch.
 // The only waits are the bounded mbarrier waits of the bulk-copy pipeline
 // (below). The schedule (chunk bytes, slab bytes, CTAs per SM) comes from an
 // autotuner whose choices are cached per shape class in a text file next to
@@ -41,7 +41,7 @@ struct nca_batch {
   // device tables
   void* d_items = nullptr;    // ItemDev[n]
   void* d_chunks = nullptr;   // ChunkDev[nchunks]
-  void* d_parts = nullptr;    // PartDev[nchunks]
+  void* d_parts = nullptr;    // PartDev[nchunks * consumer warps]
   void* d_done = nullptr;     // unsigned[n]
   void* d_status = nullptr;   // int: NCA_ERR_TIMEOUT after a wait that ran out
   long long nchunks = 0;
@@ -111,16 +111,27 @@ struct FF2 {
   }
 };
 
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 struct Acc2 {
   FF2 s, q;
   float mx = -3.40282347e+38f;   // lowest float (bit pattern 0xff7fffff)
-  // a pair of elements (a missing one is passed as 0 with `two` false)
-  __device__ __forceinline__ void see(float2 x, bool two = true) {
+  // a pair of elements
+  __device__ __forceinline__ void see(float2 x) {
     s.add(x);
     const float2 nx = make_float2(-x.x, -x.y);
     q.add(__ffma2_rn(x, x, nx));
-    mx = fmaxf(mx, x.x);
-    if (two) mx = fmaxf(mx, x.y);
+    mx = max3f(mx, x.x, x.y);
+  }
+  // one element (the other lane adds zero)
+  __device__ __forceinline__ void see1(float x) {
+    s.add(make_float2(x, 0.f));
+    q.add(make_float2(__fmaf_rn(x, x, -x), 0.f));
+    mx = fmaxf(mx, x);
   }
 };
 
@@ -164,14 +175,7 @@ template <> struct Vec<NCA_FLOAT16> {
   }
 };
 
-// ---- the persistent kernel --------------------------------------------------------
-// Every CTA walks its chunks (blockIdx.x, + gridDim.x, ...). A chunk's 16-byte
-// aligned body streams through NSLAB shared-memory slabs of `slab` bytes filled
-// by cp.async.bulk (thread 0 keeps NSLAB slabs in flight, across chunk
-// boundaries, completion on one mbarrier per slab); the unaligned head and
-// tail (< 16 bytes each) are read with plain loads. Waits are bounded (2 s of
-// %globaltimer): on a timeout the CTA records NCA_ERR_TIMEOUT in the batch
-// status word, waits (bounded) for its copies in flight and stops.
+// bulk-copy slabs per CTA and the limit of every wait on one of their mbarriers
 constexpr int NSLAB = 4;
 constexpr unsigned long long kWaitNs = 2000000000ull;
 
@@ -209,11 +213,11 @@ __device__ __forceinline__ void see_vec(Acc2& acc, const uint4& u) {
   for (int j = 0; j < Vec<DT>::kElems / 2; ++j) acc.see(f[j]);
 }
 
-// two accumulator sets take alternate vectors: two independent TwoSum chains
+// two accumulator sets take alternate vectors: two independent TwoSum chains.
+// t: this thread's index among the T consumer threads
 template <int DT>
-__device__ __forceinline__ void see_slab(Acc2& a0, Acc2& a1, const uint4* v, int nv) {
-  const int T = blockDim.x;
-  int i = threadIdx.x;
+__device__ __forceinline__ void see_slab(Acc2& a0, Acc2& a1, const uint4* v, int nv, int t, int T) {
+  int i = t;
   for (; i + T < nv; i += 2 * T) {
     const uint4 u0 = v[i], u1 = v[i + T];
     see_vec<DT>(a0, u0);
@@ -222,140 +226,189 @@ __device__ __forceinline__ void see_slab(Acc2& a0, Acc2& a1, const uint4* v, int
   if (i < nv) see_vec<DT>(a0, v[i]);
 }
 
-// head and tail elements of chunk c outside its aligned body
-__device__ __forceinline__ void see_edges(Acc2& acc, const ItemDev& it, const ChunkDev& c, const Body& b) {
+// head and tail elements of chunk c outside its aligned body (one warp: < 16 elements)
+__device__ __forceinline__ void see_edges(Acc2& acc, const ItemDev& it, const ChunkDev& c, const Body& b, int lane) {
   const int isz = it.dtype == NCA_FLOAT32 ? 4 : 2;
   const uintptr_t lo = (uintptr_t)it.data + (uintptr_t)(c.begin * isz);
   const long long nh = (long long)((b.a - lo) / isz);               // elements before the body
   const long long nt = c.count - nh - (long long)((b.e - b.a) / isz);  // elements after it
-  for (long long t = threadIdx.x; t < nh + nt; t += blockDim.x) {
+  for (long long t = lane; t < nh + nt; t += 32) {
     const long long i = t < nh ? c.begin + t : c.begin + c.count - nt + (t - nh);
-    acc.see(make_float2(ld_elem(it.data, i, it.dtype), 0.f), false);
+    acc.see1(ld_elem(it.data, i, it.dtype));
   }
 }
 
-// block tree of a chunk's accumulators into a PartDev (valid in thread 0)
-__device__ PartDev block_part(const Acc2& acc, const Acc2& acc1) {
-  double ds = acc.s.get() + acc1.s.get(), dq = acc.q.get() + acc1.q.get();
-  float mx = fmaxf(acc.mx, acc1.mx);
+// float-float addition of two (hi, lo) pairs, both lanes at once (Knuth TwoSum
+// of the highs, the lows added to its error, Fast2Sum renormalisation)
+__device__ __forceinline__ void ff2_add(float2& h, float2& l, float2 h2, float2 l2) {
+  const float2 m1 = make_float2(-1.f, -1.f);
+  const float2 s = __fadd2_rn(h, h2);
+  const float2 bb = __ffma2_rn(h, m1, s);
+  const float2 e1 = __ffma2_rn(__ffma2_rn(bb, m1, s), m1, h);
+  const float2 e2 = __ffma2_rn(bb, m1, h2);
+  const float2 e = __fadd2_rn(__fadd2_rn(e1, e2), __fadd2_rn(l, l2));
+  const float2 hi = __fadd2_rn(s, e);
+  l = __ffma2_rn(__ffma2_rn(s, m1, hi), m1, e);
+  h = hi;
+}
+
+__device__ __forceinline__ float2 shfl_down2(float2 v, int off) {
+  return make_float2(__shfl_down_sync(0xffffffffu, v.x, off), __shfl_down_sync(0xffffffffu, v.y, off));
+}
+
+// a warp's accumulators -> one partial (valid in lane 0). float32 float-float
+// all the way down the warp tree; float64 only for lane 0's final conversion.
+__device__ PartDev warp_part(const Acc2& a0, const Acc2& a1) {
+  float2 sh = a0.s.hi, sl = a0.s.lo, qh = a0.q.hi, ql = a0.q.lo;
+  ff2_add(sh, sl, a1.s.hi, a1.s.lo);
+  ff2_add(qh, ql, a1.q.hi, a1.q.lo);
+  // lanes now (even, odd) elements; regroup as (sum, sum_sq_m) and add the halves
+  float2 h = make_float2(sh.x, qh.x), l = make_float2(sl.x, ql.x);
+  ff2_add(h, l, make_float2(sh.y, qh.y), make_float2(sl.y, ql.y));
+  float mx = fmaxf(a0.mx, a1.mx);
   for (int off = 16; off > 0; off >>= 1) {
-    ds += __shfl_down_sync(0xffffffffu, ds, off);
-    dq += __shfl_down_sync(0xffffffffu, dq, off);
+    const float2 h2 = shfl_down2(h, off), l2 = shfl_down2(l, off);
+    ff2_add(h, l, h2, l2);
     mx = fmaxf(mx, __shfl_down_sync(0xffffffffu, mx, off));
   }
-  __shared__ double sh_s[32], sh_q[32];
-  __shared__ float sh_m[32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  __syncthreads();
-  if (lane == 0) { sh_s[wid] = ds; sh_q[wid] = dq; sh_m[wid] = mx; }
-  __syncthreads();
-  PartDev p{0.0, 0.0, lowest_f(), 0};
-  if (threadIdx.x == 0) {
-    for (int k = 0; k < nw; ++k) {   // fixed order: deterministic
-      p.s += sh_s[k];
-      p.q += sh_q[k];
-      p.mx = fmaxf(p.mx, sh_m[k]);
-    }
-  }
+  PartDev p;
+  p.s = (double)h.x + (double)l.x;
+  p.q = (double)h.y + (double)l.y;
+  p.mx = mx;
+  p.pad = 0;
   return p;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// ---- the persistent kernel --------------------------------------------------------
+// blockDim = consumer threads + one producer warp (the last warp). The
+// producer's lane 0 walks this CTA's chunk sequence issuing one bulk copy per
+// slab into NSLAB shared-memory slabs; slab k completes on full[k] (transaction
+// bytes) and is released on empty[k] once every consumer warp has read it
+// (one arrival per warp), so consumer warps run without block barriers. Each
+// consumer warp reduces its share of every slab, writes one partial per chunk
+// (parts[chunk * NW + warp]) and counts it on the array's counter; the warp
+// that brings the count to nchunks * NW merges the array's partials in a fixed
+// order (float64; deterministic) and resets the counter for the next launch.
+// Waits are bounded (2 s of %globaltimer); a wait that runs out records
+// NCA_ERR_TIMEOUT, raises the CTA's stop flag, and the producer then waits
+// (bounded) for its copies in flight before the CTA exits.
 __global__ void batch_persistent_kernel(const ItemDev* __restrict__ items, const ChunkDev* __restrict__ chunks,
                                         long long nchunks, PartDev* __restrict__ parts, unsigned* __restrict__ done,
                                         nca_batch_result* __restrict__ results, int slab, int* __restrict__ status) {
   extern __shared__ __align__(128) unsigned char sm[];
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
-  const uint32_t bbase = sbase + NSLAB * slab;
-  __shared__ int s_last;
+  const uint32_t full0 = sbase + NSLAB * slab;   // full[k] at full0 + 8k, empty[k] at full0 + 8(NSLAB + k)
+  const uint32_t empty0 = full0 + 8 * NSLAB;
+  __shared__ volatile int s_stop;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int T = (int)blockDim.x - 32, NW = T >> 5;   // consumer threads and warps
   if (threadIdx.x == 0) {
-    for (int k = 0; k < NSLAB; ++k) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bbase + 8 * k) : "memory");
+    s_stop = 0;
+    for (int k = 0; k < NSLAB; ++k) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * k) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(empty0 + 8 * k), "r"(NW) : "memory");
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  // producer cursor (thread 0): next (chunk, slab) to issue and slabs issued
-  long long pc = blockIdx.x, ps = 0, issued = 0;
-  Body pb{0, 0, 0};
-  if (threadIdx.x == 0 && pc < nchunks) pb = chunk_body(chunks[pc]);
-  auto advance = [&]() {   // to the next slab of this CTA's sequence, if any
-    while (pc < nchunks) {
-      if (ps < pb.slabs) return true;
-      pc += gridDim.x;
-      ps = 0;
-      if (pc < nchunks) pb = chunk_body(chunks[pc]);
+
+  if (wid == NW) {   // producer warp
+    if (lane != 0) return;
+    long long issued = 0;
+    bool failed = false;
+    for (long long c = blockIdx.x; c < nchunks && !failed; c += gridDim.x) {
+      const Body bd = chunk_body(chunks[c]);
+      for (long long i = 0; i < bd.slabs; ++i, ++issued) {
+        const int k = (int)(issued % NSLAB);
+        if (issued >= NSLAB &&
+            !mbar_wait(empty0 + 8 * k, (uint32_t)((issued / NSLAB - 1) & 1), kWaitNs)) {
+          failed = true;
+          break;
+        }
+        if (s_stop) { failed = true; break; }
+        const uintptr_t src = bd.a + (uintptr_t)i * slab;
+        const uintptr_t left = bd.e - src;
+        const uint32_t bytes = (uint32_t)(left < (uintptr_t)slab ? left : (uintptr_t)slab);
+        const uint32_t bar = full0 + 8 * k;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(sbase + (uint32_t)(k * slab)), "l"(src), "r"(bytes), "r"(bar) : "memory");
+      }
     }
-    return false;
-  };
-  auto issue = [&]() {
-    const Body& bd = pb;
-    const uintptr_t src = bd.a + (uintptr_t)ps * slab;
-    const uintptr_t left = bd.e - src;
-    const uint32_t bytes = (uint32_t)(left < (uintptr_t)slab ? left : (uintptr_t)slab);
-    const int k = (int)(issued % NSLAB);
-    const uint32_t bar = bbase + 8 * k;
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                 ::"r"(sbase + (uint32_t)(k * slab)), "l"(src), "r"(bytes), "r"(bar) : "memory");
-    ++issued;
-    ++ps;
-  };
-  if (threadIdx.x == 0)
-    for (int k = 0; k < NSLAB && advance(); ++k) issue();
+    if (failed) {
+      atomicExch(status, (int)NCA_ERR_TIMEOUT);
+      s_stop = 1;
+      // the copies still in flight land before the CTA (and its shared memory) goes away
+      for (long long j = issued > NSLAB ? issued - NSLAB : 0; j < issued; ++j)
+        mbar_wait(full0 + 8 * (int)(j % NSLAB), (uint32_t)((j / NSLAB) & 1), kWaitNs / 2);
+    }
+    return;
+  }
+
+  // consumer warps
   long long consumed = 0;
-  bool failed = false;
-  for (long long c = blockIdx.x; c < nchunks && !failed; c += gridDim.x) {
+  for (long long c = blockIdx.x; c < nchunks; c += gridDim.x) {
     const ChunkDev ch = chunks[c];
     const ItemDev it = items[ch.item];
     const Body bd = chunk_body(ch);
     Acc2 acc, acc1;
-    see_edges(acc, it, ch, bd);
+    if (wid == 0) see_edges(acc, it, ch, bd, lane);
     for (long long i = 0; i < bd.slabs; ++i, ++consumed) {
       const int k = (int)(consumed % NSLAB);
-      const bool ok = mbar_wait(bbase + 8 * k, (uint32_t)((consumed / NSLAB) & 1), kWaitNs);
-      if (__syncthreads_or(ok ? 0 : 1)) { failed = true; break; }
+      if (!mbar_wait(full0 + 8 * k, (uint32_t)((consumed / NSLAB) & 1), kWaitNs) || s_stop) {
+        if (lane == 0) { atomicExch(status, (int)NCA_ERR_TIMEOUT); s_stop = 1; }
+        return;
+      }
       const uintptr_t src = bd.a + (uintptr_t)i * slab;
       const uintptr_t left = bd.e - src;
       const int nv = (int)((left < (uintptr_t)slab ? left : (uintptr_t)slab) / 16);
       const uint4* v = reinterpret_cast<const uint4*>(sm + k * slab);
-      if (it.dtype == NCA_FLOAT32) see_slab<NCA_FLOAT32>(acc, acc1, v, nv);
-      else if (it.dtype == NCA_BFLOAT16) see_slab<NCA_BFLOAT16>(acc, acc1, v, nv);
-      else see_slab<NCA_FLOAT16>(acc, acc1, v, nv);
-      __syncthreads();   // slab k is free again
-      if (threadIdx.x == 0 && advance()) issue();
+      if (it.dtype == NCA_FLOAT32) see_slab<NCA_FLOAT32>(acc, acc1, v, nv, threadIdx.x, T);
+      else if (it.dtype == NCA_BFLOAT16) see_slab<NCA_BFLOAT16>(acc, acc1, v, nv, threadIdx.x, T);
+      else see_slab<NCA_FLOAT16>(acc, acc1, v, nv, threadIdx.x, T);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(empty0 + 8 * k);   // this warp is done with slab k
     }
-    if (failed) break;
-    const PartDev p = block_part(acc, acc1);
-    if (threadIdx.x == 0) {
-      parts[c] = p;
+    const PartDev p = warp_part(acc, acc1);
+    const unsigned want = (unsigned)it.nchunks * (unsigned)NW;
+    unsigned prev = 0;
+    if (lane == 0) {
+      parts[c * NW + wid] = p;
       __threadfence();
-      const unsigned prev = atomicAdd(done + ch.item, 1u);
-      s_last = (prev + 1 == (unsigned)it.nchunks) ? 1 : 0;
+      prev = atomicAdd(done + ch.item, 1u);
     }
-    __syncthreads();
-    if (s_last && threadIdx.x == 0) {
+    prev = __shfl_sync(0xffffffffu, prev, 0);
+    if (prev + 1 == want) {   // this warp merges the array: lanes take partials in a fixed order
       __threadfence();
       double s = 0.0, q = 0.0;
       float mx = lowest_f();
-      for (int k = 0; k < it.nchunks; ++k) {   // chunk order; L2 reads (written by other SMs)
-        const PartDev* pk = parts + it.first_chunk + k;
-        s += __ldcg(&pk->s);
-        q += __ldcg(&pk->q);
-        const float m = __ldcg(&pk->mx);
+      const PartDev* pk = parts + (long long)it.first_chunk * NW;
+      for (unsigned j = lane; j < want; j += 32) {
+        s += __ldcg(&pk[j].s);
+        q += __ldcg(&pk[j].q);
+        const float m = __ldcg(&pk[j].mx);
         mx = m > mx ? m : mx;
       }
-      nca_batch_result r;
-      r.sum = s;
-      r.mean = s / (double)it.length;
-      r.max = (double)mx;
-      r.sum_sq_m = q;
-      results[ch.item] = r;
-      done[ch.item] = 0u;   // ready for the next launch
+      for (int off = 16; off > 0; off >>= 1) {
+        s += __shfl_down_sync(0xffffffffu, s, off);
+        q += __shfl_down_sync(0xffffffffu, q, off);
+        const float m = __shfl_down_sync(0xffffffffu, mx, off);
+        mx = m > mx ? m : mx;
+      }
+      if (lane == 0) {
+        nca_batch_result r;
+        r.sum = s;
+        r.mean = s / (double)it.length;
+        r.max = (double)mx;
+        r.sum_sq_m = q;
+        results[ch.item] = r;
+        done[ch.item] = 0u;   // ready for the next launch
+      }
     }
-    __syncthreads();
-  }
-  if (failed && threadIdx.x == 0) {
-    atomicExch(status, (int)NCA_ERR_TIMEOUT);
-    for (long long k = consumed; k < issued; ++k)
-      mbar_wait(bbase + 8 * (int)(k % NSLAB), (uint32_t)((k / NSLAB) & 1), kWaitNs / 2);
   }
 }
 
@@ -413,10 +466,10 @@ void launch_persistent(nca_batch* B, nca_batch_result* results, cudaStream_t s) 
   const ChunkDev* ch = (const ChunkDev*)B->d_chunks;
   PartDev* pa = (PartDev*)B->d_parts;
   unsigned* dn = (unsigned*)B->d_done;
-  const int smem = NSLAB * B->slab + 8 * NSLAB;
+  const int smem = NSLAB * B->slab + 16 * NSLAB;
   nca::check_cuda(cudaFuncSetAttribute(batch_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
                   "batch smem");
-  batch_persistent_kernel<<<grid, B->threads, smem, s>>>(it, ch, B->nchunks, pa, dn, results, B->slab,
+  batch_persistent_kernel<<<grid, B->threads + 32, smem, s>>>(it, ch, B->nchunks, pa, dn, results, B->slab,
                                                          (int*)B->d_status);
   nca::check_cuda(cudaGetLastError(), "batched kernel launch");
   nca::count_launch();
@@ -473,7 +526,8 @@ void build_chunks(nca_batch* B, cudaStream_t s) {
     check_cuda(cudaMemsetAsync(B->d_status, 0, sizeof(int), s), "batch status");
   }
   check_cuda(cudaMalloc(&B->d_chunks, sizeof(ChunkDev) * std::max<long long>(B->nchunks, 1)), "batch chunks");
-  check_cuda(cudaMalloc(&B->d_parts, sizeof(PartDev) * std::max<long long>(B->nchunks, 1)), "batch partials");
+  check_cuda(cudaMalloc(&B->d_parts, sizeof(PartDev) * std::max<long long>(B->nchunks, 1) * (B->threads / 32)),
+             "batch partials");
   check_cuda(cudaMemcpyAsync(B->d_items, items.data(), sizeof(ItemDev) * B->n, cudaMemcpyHostToDevice, s), "items");
   check_cuda(cudaMemcpyAsync(B->d_chunks, chunks.data(), sizeof(ChunkDev) * B->nchunks, cudaMemcpyHostToDevice, s),
              "chunks");
@@ -495,11 +549,11 @@ std::string shape_class(const nca_batch* B) {
 }
 
 // lines "<shape class> <chunk bytes> <threads> <slab bytes> <ctas per sm>"
-std::string tune_file() { return nca::jit_cache_dir() + "/batch_tune_bulk.txt"; }
+std::string tune_file() { return nca::jit_cache_dir() + "/batch_tune_ws.txt"; }
 
 bool schedule_ok(long long cb, int th, int slab, int cps) {
   return cb >= (64ll << 10) && (th == 256 || th == 512) && (slab == 8192 || slab == 16384 || slab == 32768) &&
-         cps >= 1 && cps <= 8 && (long long)cps * NSLAB * slab <= 200ll * 1024 && th * cps <= 2048;
+         cps >= 1 && cps <= 8 && (long long)cps * NSLAB * slab <= 200ll * 1024 && (th + 32) * cps <= 2048;
 }
 
 bool load_tuned(nca_batch* B) {
@@ -622,10 +676,19 @@ int32_t nca_batch_autotune(nca_batch* B, nca_batch_result* results, void* stream
     cudaStream_t s = (cudaStream_t)stream;
     struct Cand { long long cb; int th, sl, cps; };
     std::vector<Cand> cands;
+    check_cuda(cudaFuncSetAttribute(batch_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    NSLAB * 32768 + 16 * NSLAB),
+               "batch smem");
     for (long long cb : {256ll << 10, 512ll << 10, 1024ll << 10})
       for (int sl : {8192, 16384, 32768})
-        for (int cps : {2, 3, 4})
-          if (schedule_ok(cb, 256, sl, cps)) cands.push_back({cb, 256, sl, cps});
+        for (int cps : {2, 3, 4}) {
+          int resident = 0;   // CTAs of this shape that fit on an SM at once
+          check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, batch_persistent_kernel, 256 + 32,
+                                                                   NSLAB * sl + 16 * NSLAB),
+                     "occupancy");
+          if (schedule_ok(cb, 256, sl, cps) && resident >= cps) cands.push_back({cb, 256, sl, cps});
+        }
+    if (cands.empty()) cands.push_back({256ll << 10, 256, 16384, 3});
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "event");
     check_cuda(cudaEventCreate(&e1), "event");
