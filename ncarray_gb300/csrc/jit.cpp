@@ -541,6 +541,8 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
   // the staged class asks for sp.minb resident CTAs per SM (register cap)
   if (sp.kind == 6 && sp.minb > 1) os << "#define NCA_LB 256, " << sp.minb << "\n";
   else os << "#define NCA_LB 256\n";
+  // kind 7: CTAs per SM its shared memory allows (the register cap follows)
+  if (sp.kind == 7) os << "#define NCA_K7_MINB " << std::max(1, sp.minb) << "\n";
   os << "#define NCA_GRP " << sp.grp << "\n";
   os << "#define NCA_QD " << sp.qd << "\n#define NCA_QXP " << sp.qxp << "\n#define NCA_QX " << sp.qx << "\n#define NCA_TP " << sp.tp
      << "\n#define NCA_RB " << sp.rb << "\n#define NCA_TMASK " << sp.tmask << "u\n#define NCA_TILE_BYTES "
@@ -1109,24 +1111,31 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   }
   if (sp.has_out && !tma_ok(s.out, false)) return false;
   // block of rb loop indices: a divisor of the fastest loop extent whose
-  // (loop index, q) rows fill whole 128-byte boxes, at most 128 of them
-  // 64 (loop index, q) rows per block and 3 stages measured best on the C2
-  // views (about 65 KiB per CTA, so three CTAs share an SM)
-  int rb = 0, rb_max = (int)std::max<int64_t>(1, 64 / QX);
-  if (const char* e = getenv("NCA_STAGED_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) rb_max = v; }
-  for (int c = 16; c >= 1; c /= 2)
-    if (c <= rb_max && LX % c == 0 && c * QX <= 128 && (c * QX) % 32 == 0) { rb = c; break; }
-  if (rb == 0) return false;
-  const int tp = 32, rowq = rb * (int)QX;
-  const int64_t xt = (int64_t)(rowq / 32) * tp * 128, kt = (int64_t)rowq * 128;
-  const int64_t stage = nt * xt + npc * kt;
-  // as many stages (2..6) as fit in the 227 KiB a CTA may use
+  // (loop index, q) rows fill whole 128-byte boxes, at most 128 of them, the
+  // largest whose stages fit in the 227 KiB a CTA may use. 128 rows per block
+  // and 2 stages measured best on the C2 views (about 97 KiB per CTA, two
+  // CTAs per SM: 5.6 TB/s against 5.4 TB/s for 64 rows and 3 stages, three
+  // CTAs per SM)
   const int64_t budget = 227 * 1024;
-  int ns = 3;
-  auto smem_of = [&](int n) { return n * stage + 2 * kt + 8 * n + 1024; };
-  if (const char* e = getenv("NCA_STAGED_STAGES")) { const int v = atoi(e); if (v >= 2 && v <= 6) ns = v; }
-  while (ns > 2 && smem_of(ns) > budget) --ns;
-  if (smem_of(ns) > budget) return false;
+  const int tp = 32;
+  int rb_max = (int)std::max<int64_t>(1, 128 / QX);
+  if (const char* e = getenv("NCA_STAGED_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) rb_max = v; }
+  int ns_want = 2;
+  if (const char* e = getenv("NCA_STAGED_STAGES")) { const int v = atoi(e); if (v >= 2 && v <= 6) ns_want = v; }
+  // stages, two output tiles, full/empty mbarriers per stage and two per output tile
+  auto smem_for = [&](int c, int n) {
+    const int64_t rq = (int64_t)c * QX;
+    const int64_t stage = nt * ((rq / 32) * tp * 128) + npc * (rq * 128);
+    return n * stage + 2 * (rq * 128) + 16 * n + 32 + 1024;
+  };
+  int rb = 0, ns = 2;
+  for (int c = 16; c >= 1 && rb == 0; c /= 2) {
+    if (c > rb_max || LX % c != 0 || c * QX > 128 || (c * QX) % 32 != 0) continue;
+    for (int n = ns_want; n >= 2; --n)
+      if (smem_for(c, n) <= budget) { rb = c; ns = n; break; }
+  }
+  if (rb == 0) return false;
+  auto smem_of = [&](int n) { return smem_for(rb, n); };
   const unsigned smem = (unsigned)smem_of(ns);
   sp.kind = 7;
   sp.nd = s.nd;
@@ -1143,7 +1152,10 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   sp.qd = qd; sp.qx = (int)QX; sp.qxp = qxp; sp.tp = tp; sp.rb = rb; sp.tmask = tmask; sp.tile_bytes = 0;
   sp.ns = ns; sp.ld = ld; sp.npc = npc; sp.pmask = pmask; sp.umask = umask; sp.uumask = uumask; sp.ltp8 = 2;
   sp.nmaps = nt + npc + (sp.has_out ? 1 : 0);
-  sp.minb = 1; sp.grp = 1;
+  // as many CTAs per SM as their shared memory allows (228 KiB per SM, 1 KiB
+  // reserved per CTA), at most three: ptxas caps the registers to match
+  sp.minb = (int)std::max<int64_t>(1, std::min<int64_t>(3, (228 * 1024) / ((int64_t)smem + 1024)));
+  sp.grp = 1;
   // tensor maps: staged operands, p operands, the stored value
   struct Maps { CUtensorMap m[NCA_MAX_OPERANDS + 1]; };
   Maps maps;
@@ -1182,7 +1194,9 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   const int sms = sm_count(current_device());
   int per_sm = 0;
   check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem), "smem attribute");
-  check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem), "occupancy");
+  // 8 consumer warps, a load warp and (when a value is stored) a store warp
+  const int threads = 256 + 32 + (sp.has_out ? 32 : 0);
+  check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem), "occupancy");
   if (per_sm < 1) return false;
   const int64_t U = KN / ((int64_t)tp * QX), NB = RN / rb, W = U * NB;
   const int64_t G = std::min<int64_t>((int64_t)sms * per_sm, W);
@@ -1210,7 +1224,7 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   memcpy(mpa, &maps, sizeof(CUtensorMap) * sp.nmaps);
   void* params[] = {w.data(), mpa};
   count_launch();
-  check_cu(drv().cuLaunchKernel(fn, (unsigned)G, 1, 1, 256, 1, 1, smem, (CUstream)stream, params, nullptr),
+  check_cu(drv().cuLaunchKernel(fn, (unsigned)G, 1, 1, (unsigned)threads, 1, 1, smem, (CUstream)stream, params, nullptr),
            "cuLaunchKernel");
   return true;
 }
@@ -1631,8 +1645,8 @@ int jit_selftest(const char* arch) {
       a7.op_dtypes = {d[2], d[2], d[2]};
       a7.op_modes = {M_STAGED, M_CONTIG, M_CONST};
       a7.has_out = true; a7.nred = 2; a7.red_ops = 2u | (4u << 4); a7.has_max = true;
-      a7.kept_mask = 1u | 2u | 8u; a7.qd = 0; a7.qx = 8; a7.qxp = 8; a7.tp = 32; a7.ltp8 = 2; a7.rb = 16;
-      a7.tmask = 1u; a7.pmask = 2u; a7.umask = 4u; a7.npc = 1; a7.ns = 4; a7.ld = 2; a7.nmaps = 3;
+      a7.kept_mask = 1u | 2u | 8u; a7.qd = 0; a7.qx = 8; a7.qxp = 8; a7.tp = 32; a7.ltp8 = 2; a7.rb = 8;
+      a7.tmask = 1u; a7.pmask = 2u; a7.umask = 4u; a7.npc = 1; a7.ns = 3; a7.ld = 2; a7.nmaps = 3; a7.minb = 3;
       nvrtc_compile(gen_source(a7, t), a);
       ++n;
       a7.nred = 0; a7.red_ops = 0; a7.has_max = false; a7.kept_mask = 1u | 8u;
