@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "common.hpp"
+#include "mbar.cuh"
 #include "jit.hpp"
 
 struct nca_batch {
@@ -179,23 +180,9 @@ template <> struct Vec<NCA_FLOAT16> {
 constexpr int NSLAB = 4;
 constexpr unsigned long long kWaitNs = 2000000000ull;
 
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
-  const unsigned long long t0 = gtimer();
-  while (true) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
-    if (ok) return true;
-    if (gtimer() - t0 > limit_ns) return false;
-  }
-}
+using nca_dev::gtimer;
+using nca_dev::mbar_wait;
 
 // the 16-byte aligned body of a chunk (computed on the host)
 struct Body {

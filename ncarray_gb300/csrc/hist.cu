@@ -37,6 +37,7 @@
 #include <cstdint>
 
 #include "common.hpp"
+#include "mbar.cuh"
 
 namespace {
 
@@ -169,23 +170,9 @@ tile_plan_kernel(const unsigned* __restrict__ est, int nv, long long* __restrict
 // while the current one is binned. Waits are bounded (2 s of %globaltimer):
 // on a timeout the CTA records NCA_ERR_TIMEOUT, waits for its copies in
 // flight and stops. CTA c appends to sub-bucket c % NSUB of every tile.
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
-  const unsigned long long t0 = gtimer();
-  while (true) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
-    if (ok) return true;
-    if (gtimer() - t0 > limit_ns) return false;
-  }
-}
+using nca_dev::gtimer;
+using nca_dev::mbar_wait;
 
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"

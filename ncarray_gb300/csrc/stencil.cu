@@ -23,6 +23,7 @@
 #include <mutex>
 
 #include "common.hpp"
+#include "mbar.cuh"
 
 namespace {
 
@@ -44,23 +45,9 @@ template <class T> __host__ __device__ constexpr int stage_bytes() {
   return ((box_w<T>() * (TY + 2) * (int)sizeof(T)) + 127) / 128 * 128;
 }
 
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
-  const unsigned long long t0 = gtimer();
-  while (true) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
-    if (ok) return true;
-    if (gtimer() - t0 > limit_ns) return false;
-  }
-}
+using nca_dev::gtimer;
+using nca_dev::mbar_wait;
 
 template <class T>
 __device__ __forceinline__ void issue_plane(const CUtensorMap* tmap, uint32_t dst, uint32_t bar, int x, int y, int z) {
