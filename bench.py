@@ -748,74 +748,96 @@ def main():
         # streams: host->device copies of chunk i+1, the fused and int32
         # expressions of chunk i and device->host copies of chunk i-1 overlap
         # (host<->device copies of strided chunk views through nca_copy_host)
-        NCH = int(os.environ.get("NCA_E2E_CHUNKS", "8"))
+        NCH = int(os.environ.get("NCA_E2E_CHUNKS", "2"))
         NCS = int(os.environ.get("NCA_E2E_COPY_STREAMS", "1"))
         bc = 256 // NCH
         hx4, hk4 = hx.view(64, 256, 256, 8), hk.view(8, 256, 256, 64)
         hy4, hz4 = hy.view(8, 256, 256, 64), hz.view(8, 256, 256, 64)
         hm3, ha3 = hm.view(8, 256, 64), ha.view(8, 256, 64)
-        parts = []
-        for i in range(NCH):
-            b0, b1 = i * bc, (i + 1) * bc
-            dxc, dvc, dkc = dx[:, b0:b1], dv[b0:b1], dk[:, b0:b1]
-            with nca.lazy_mode():
-                ye = dxc.permute(3, 1, 2, 0) * dvc.reshape(1, bc, 1, 1) + dkc
-                ze = (dkc * 3 + 7) % 11
-            parts.append(dict(dx=dxc, dv=dvc, dk=dkc, ye=ye, ze=ze, y=step.y[:, b0:b1], z=step.z[:, b0:b1],
-                              mx=step.mx[:, b0:b1], am=step.am[:, b0:b1], hx=hx4[:, b0:b1], hv=hv[b0:b1],
-                              hk=hk4[:, b0:b1], hy=hy4[:, b0:b1], hz=hz4[:, b0:b1], hm=hm3[:, b0:b1],
-                              ha=ha3[:, b0:b1]))
+        red = [(nca.RedOp.MAX, 2), (nca.RedOp.ARGMAX, 2)]
+
+        def chunk_parts(bx, bv, bk, by_, bz, bm, ba):
+            """the NCH chunk views of one set of device buffers"""
+            out = []
+            for i in range(NCH):
+                b0, b1 = i * bc, (i + 1) * bc
+                dxc, dvc, dkc = bx[:, b0:b1], bv[b0:b1], bk[:, b0:b1]
+                with nca.lazy_mode():
+                    ye = dxc.permute(3, 1, 2, 0) * dvc.reshape(1, bc, 1, 1) + dkc
+                    ze = (dkc * 3 + 7) % 11
+                out.append(dict(dx=dxc, dv=dvc, dk=dkc, ye=ye, ze=ze, y=by_[:, b0:b1], z=bz[:, b0:b1],
+                                mx=bm[:, b0:b1], am=ba[:, b0:b1], hx=hx4[:, b0:b1], hv=hv[b0:b1],
+                                hk=hk4[:, b0:b1], hy=hy4[:, b0:b1], hz=hz4[:, b0:b1], hm=hm3[:, b0:b1],
+                                ha=ha3[:, b0:b1]))
+            return out
+
+        # two sets of device buffers: consecutive steps alternate between them,
+        # so a step waits only for the step two back to release its buffers
+        sets = [chunk_parts(dx, dv, dk, step.y, step.z, step.mx, step.am)]
+        sets.append(chunk_parts(nca.NCDevArray(dx.shape, dx.dtype), nca.NCDevArray(dv.shape, dv.dtype),
+                                nca.NCDevArray(dk.shape, dk.dtype), nca.NCDevArray(step.y.shape, step.y.dtype),
+                                nca.NCDevArray(step.z.shape, step.z.dtype), nca.NCDevArray(step.mx.shape, step.mx.dtype),
+                                nca.NCDevArray(step.am.shape, step.am.dtype)))
         s_ins = [torch.cuda.Stream() for _ in range(NCS)]
         s_outs = [torch.cuda.Stream() for _ in range(NCS)]
         s_cmp = torch.cuda.Stream()
-        ev_in = [torch.cuda.Event() for _ in range(NCH)]
-        ev_cmp = [torch.cuda.Event() for _ in range(NCH)]
-        ev_out = [torch.cuda.Event() for _ in range(NCH)]
-        red = [(nca.RedOp.MAX, 2), (nca.RedOp.ARGMAX, 2)]
+        ev_in = [[torch.cuda.Event() for _ in range(NCH)] for _ in sets]
+        ev_cmp = [[torch.cuda.Event() for _ in range(NCH)] for _ in sets]
+        ev_out = [[torch.cuda.Event() for _ in range(NCH)] for _ in sets]
 
-        def e2e_pipelined(cross_step=True):
+        def e2e_pipelined(cross_step=True, nsteps=1):
+            """nsteps steps, each copying all its inputs in and all its results
+            out; step r uses buffer set r % 2. With cross_step the first steps
+            also wait for a previous call's use of their set (later steps always
+            wait for the step two back)."""
             cur = torch.cuda.current_stream()
             for st in s_ins + s_outs + [s_cmp]:
                 st.wait_stream(cur)
-            for i, c in enumerate(parts):
-                s_in, s_out = s_ins[i % NCS], s_outs[i % NCS]
-                with torch.cuda.stream(s_in):
-                    if cross_step:
-                        s_in.wait_event(ev_cmp[i])      # the previous step is done reading chunk i
-                    c["dx"].copy_from(c["hx"])
-                    c["dv"].copy_from(c["hv"])
-                    c["dk"].copy_from(c["hk"])
-                    ev_in[i].record(s_in)
-                with torch.cuda.stream(s_cmp):
-                    s_cmp.wait_event(ev_in[i])
-                    if cross_step:
-                        s_cmp.wait_event(ev_out[i])     # the previous step's results are on the host
-                    c["ye"].evaluate(out=c["y"], reductions=red, red_out=[c["mx"], c["am"]])
-                    c["ze"].evaluate(out=c["z"])
-                    ev_cmp[i].record(s_cmp)
-                with torch.cuda.stream(s_out):
-                    s_out.wait_event(ev_cmp[i])
-                    c["y"].copy_to(c["hy"])
-                    c["z"].copy_to(c["hz"])
-                    c["mx"].copy_to(c["hm"])
-                    c["am"].copy_to(c["ha"])
-                    ev_out[i].record(s_out)
-            for st in s_outs:
+            for r in range(nsteps):
+                S = r % 2 if nsteps > 1 else 0
+                cross = cross_step or r >= 2
+                for i, c in enumerate(sets[S]):
+                    s_in, s_out = s_ins[i % NCS], s_outs[i % NCS]
+                    with torch.cuda.stream(s_in):
+                        if cross:
+                            s_in.wait_event(ev_cmp[S][i])   # the step before is done reading chunk i of set S
+                        c["dx"].copy_from(c["hx"])
+                        c["dv"].copy_from(c["hv"])
+                        c["dk"].copy_from(c["hk"])
+                        ev_in[S][i].record(s_in)
+                    with torch.cuda.stream(s_cmp):
+                        s_cmp.wait_event(ev_in[S][i])
+                        if cross:
+                            s_cmp.wait_event(ev_out[S][i])  # and its results in set S are on the host
+                        c["ye"].evaluate(out=c["y"], reductions=red, red_out=[c["mx"], c["am"]])
+                        c["ze"].evaluate(out=c["z"])
+                        ev_cmp[S][i].record(s_cmp)
+                    with torch.cuda.stream(s_out):
+                        s_out.wait_event(ev_cmp[S][i])
+                        c["y"].copy_to(c["hy"])
+                        c["z"].copy_to(c["hz"])
+                        c["mx"].copy_to(c["hm"])
+                        c["am"].copy_to(c["ha"])
+                        ev_out[S][i].record(s_out)
+            for st in s_ins + s_outs + [s_cmp]:
                 cur.wait_stream(st)
 
         for _ in range(3):
             e2e_pipelined()
         torch.cuda.synchronize()
         ms_eager = time_events(torch, e2e_pipelined, reps)
-        # one pipelined step captured in a CUDA graph (replays of one graph on
-        # one stream never overlap, so the cross-step waits are not needed)
+        # GS pipelined steps captured in one CUDA graph: the host->device copies
+        # of step r + 1 overlap the device->host copies of step r (replays of
+        # one graph on one stream never overlap, so the first step of a replay
+        # needs no cross-step waits)
+        GS = int(os.environ.get("NCA_E2E_GRAPH_STEPS", "8"))
         g_e2e = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g_e2e):
-            e2e_pipelined(cross_step=False)
+            e2e_pipelined(cross_step=False, nsteps=GS)
         torch.cuda.synchronize()
         for _ in range(3):
             g_e2e.replay()
-        ms_e2e = time_events(torch, g_e2e.replay, reps)
+        ms_e2e = time_events(torch, g_e2e.replay, max(2, reps // GS)) / GS
         # the pipelined step computes the same results as the serial one
         hy_ref = hy.clone()
         e2e_step()
@@ -826,9 +848,10 @@ def main():
         same = bool(torch.equal(hy, hy_ref))
         e2e = {"value": round(by["step"] / (ms_e2e * 1e-3) / 1e9, 3), "unit": "GB/s",
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(ms_e2e, 4),
-               "how": f"one CUDA-graph replay of the step in {NCH} chunks along axis 1 pipelined over {NCS} "
-                      f"copy-in, 1 compute and {NCS} copy-out streams (pinned host buffers, nca_copy_host + "
-                      "evaluate on chunk views)",
+               "how": f"CUDA-graph replays of {GS} consecutive steps, each in {NCH} chunks along axis 1 "
+                      f"pipelined over {NCS} copy-in, 1 compute and {NCS} copy-out streams (pinned host "
+                      "buffers, nca_copy_host + evaluate on chunk views; every step copies all its inputs in "
+                      "and all its results out)",
                "serial_ms_per_step": round(ms_serial, 4), "eager_pipelined_ms_per_step": round(ms_eager, 4),
                "matches_serial": same}
 
