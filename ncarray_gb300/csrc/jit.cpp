@@ -319,7 +319,10 @@ static void ensure_nd1(Space& s) {
 // ============================================================================
 // source generation
 // ============================================================================
-enum { M_CONTIG = 0, M_CONST = 1, M_STRIDED = 2, M_STAGED = 3 };
+// M_PAIR0 / M_PAIR1: strided by two elements along the vector axis; a group's
+// elements sit at lanes 0, 2, 4, ... (or 1, 3, 5, ...) of a window of two
+// aligned vectors (kind 2)
+enum { M_CONTIG = 0, M_CONST = 1, M_STRIDED = 2, M_STAGED = 3, M_PAIR0 = 4, M_PAIR1 = 5 };
 
 struct Spec {
   int kind = 1, nops = 0, nd = 1, vec = 1, idx32 = 0, nkept = 0, team = 256;
@@ -330,6 +333,8 @@ struct Spec {
   uint32_t red_ops = 0;
   bool has_sum = false, has_max = false, has_min = false;
   std::vector<int> op_dtypes, op_modes;
+  std::vector<int> op_alias;   // M_PAIR*: earlier operand whose window loads this one shares (-1: none)
+  std::vector<int> op_salias;  // kind 2: earlier operand with the same strides (same offsets; -1: none)
   int nscal = 0;
   // kind 6 (staged transposed operands)
   int qd = 0, qx = 1, qxp = 1, tp = 64, rb = 1;
@@ -592,6 +597,23 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
       for (int q = 0; q < sp.vec; ++q)
         g << " v[" << k << "][" << q << "] = (nca_w)(" << from_bits(dt, lane_bits(bytes, es, q, "u")) << ");";
       g << " }\n";
+    } else if (mode == M_PAIR0 || mode == M_PAIR1) {
+      // the window: two aligned vectors from the group's first element (minus
+      // one element for M_PAIR1); every vector holds an element of the group
+      const int ph = mode == M_PAIR1 ? 1 : 0;
+      const int vb = es * sp.vec;
+      const int lead = (k < (int)sp.op_alias.size() && sp.op_alias[k] >= 0) ? sp.op_alias[k] : k;
+      const std::string wn = "pw" + std::to_string(lead);
+      if (lead == k) {
+        const std::string vt = vec_type(vb);
+        g << "  const " << vt << " " << wn << "_0 = *(const " << vt << "*)(" << base << " - " << ph * es << ");\n";
+        g << "  const " << vt << " " << wn << "_1 = *(const " << vt << "*)(" << base << " + " << vb - ph * es << ");\n";
+      }
+      for (int q = 0; q < sp.vec; ++q) {
+        const int j = ph + 2 * q;
+        g << "  v[" << k << "][" << q << "] = (nca_w)("
+          << from_bits(dt, lane_bits(vb, es, j % sp.vec, wn + "_" + std::to_string(j / sp.vec))) << ");\n";
+      }
     } else {
       for (int q = 0; q < sp.vec; ++q)
         g << "  v[" << k << "][" << q << "] = "
@@ -606,6 +628,11 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
   os << "__device__ __forceinline__ void nca_gather1(const NcaArgs& A, const i64* off, nca_w (*v)[NCA_VEC]) {\n"
      << g1.str() << "}\n";
   os << "#define nca_gather_ns nca_gather\n";
+  // operands whose byte offsets equal an earlier operand's (same strides)
+  os << "__device__ __forceinline__ constexpr int nca_sal(int k) {\n  return ";
+  for (int k = 0; k < (int)sp.op_salias.size(); ++k)
+    if (sp.op_salias[k] >= 0) os << "k == " << k << " ? " << sp.op_salias[k] << " : ";
+  os << "(k < 0 ? 0 : -1);\n}\n";
   os << "__device__ __forceinline__ nca_w nca_ld_op(int k, const char* p) {\n  switch (k) {\n";
   for (int k = 0; k < sp.nops; ++k) os << "    case " << k << ": return " << scalar_load(k, "p") << ";\n";
   os << "  }\n  return (nca_w)0;\n}\n";
@@ -878,6 +905,10 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   k += '|';
   for (int m : sp.op_modes) add(m);
   k += '|';
+  for (int a : sp.op_alias) add(a);
+  k += '|';
+  for (int a : sp.op_salias) add(a);
+  k += '|';
   for (uint32_t i : t.instrs) add(i);
   return k;
 }
@@ -947,6 +978,42 @@ static void plan_vec(const Space& s, Spec& sp, int max_vec_elems, bool with_out)
     bool ok = a.st[ax] == isz && aligned(a.base, vec * isz);
     for (int d = 0; d < ax && ok; ++d) if (a.st[d] % (vec * isz) != 0) ok = false;
     sp.op_modes[k] = ok ? M_CONTIG : M_STRIDED;
+  }
+}
+
+// kind 2: strided operands whose elements along the vector axis are two apart
+// read whole aligned windows of two vectors and keep every other lane
+// (M_PAIR0: from lane 0, M_PAIR1: from lane 1). A window never reaches a
+// 16-byte block without an element of the operand, so it stays inside the
+// operand's memory. Operands whose windows coincide (the even and odd
+// phases of one array, e.g. pixel-binning views) share the loads.
+static void plan_pairs(const Space& s, Spec& sp) {
+  sp.op_alias.assign(sp.nops, -1);
+  const int ax = s.nd - 1;
+  if (sp.vec < 2) return;
+  auto window = [&](int k) {
+    const int64_t es = dtinfo(s.ops[k].dtype).size;
+    return (uintptr_t)s.ops[k].base - (uintptr_t)(sp.op_modes[k] == M_PAIR1 ? es : 0);
+  };
+  for (int k = 0; k < sp.nops; ++k) {
+    if (sp.op_modes[k] != M_STRIDED) continue;
+    const CArr& a = s.ops[k];
+    if (a.ptr) continue;
+    const int64_t es = dtinfo(a.dtype).size, vb = es * sp.vec;
+    if ((vb != 8 && vb != 16) || a.st[ax] != 2 * es) continue;
+    const int64_t ph = (int64_t)((uintptr_t)a.base % (uintptr_t)vb);
+    if (ph != 0 && ph != es) continue;
+    bool ok = true;
+    for (int d = 0; d < ax && ok; ++d) if (a.st[d] % vb != 0) ok = false;
+    if (!ok) continue;
+    sp.op_modes[k] = ph == 0 ? M_PAIR0 : M_PAIR1;
+    for (int j = 0; j < k; ++j) {
+      if ((sp.op_modes[j] != M_PAIR0 && sp.op_modes[j] != M_PAIR1) || sp.op_alias[j] >= 0) continue;
+      if (dtinfo(s.ops[j].dtype).size != es || window(j) != window(k)) continue;
+      bool same = true;
+      for (int d = 0; d <= ax; ++d) if (s.ops[j].st[d] != a.st[d]) same = false;
+      if (same) { sp.op_alias[k] = j; break; }
+    }
   }
 }
 
@@ -1373,6 +1440,19 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
     for (int k = 0; k < nops; ++k) if (sp.op_modes[k] == M_STRIDED && sp.vec > 1) flat = false;
   }
   sp.kind = flat ? 1 : 2;
+  if (sp.kind == 2) {
+    plan_pairs(s, sp);
+    sp.op_salias.assign(nops, -1);
+    for (int k = 0; k < nops; ++k) {
+      if (s.ops[k].ptr) continue;
+      for (int j = 0; j < k; ++j) {
+        if (s.ops[j].ptr || sp.op_salias[j] >= 0) continue;
+        bool same = true;
+        for (int d = 0; d < s.nd; ++d) if (s.ops[j].st[d] != s.ops[k].st[d]) same = false;
+        if (same) { sp.op_salias[k] = j; break; }
+      }
+    }
+  }
   sp.unroll = flat ? (nops <= 2 ? 4 : nops <= 4 ? 2 : 1) : 1;
   const int64_t total = s.total();
   bool small_dims = true;
@@ -1657,6 +1737,19 @@ int jit_selftest(const char* arch) {
       ++n;
       ++n;
     }
+  }
+  // kind 2 with window-pair operands (phases 0 and 1, one sharing the other's
+  // loads): the pixel-binning shape, 4-byte and 2-byte elements
+  for (int dt : {NCA_FLOAT32, NCA_BFLOAT16}) {
+    Spec sp;
+    sp.kind = 2; sp.nops = 3; sp.nd = 3; sp.vec = 16 / dtinfo(dt).size; sp.idx32 = 1; sp.nscal = 1;
+    sp.w = NCA_FLOAT32; sp.r = NCA_FLOAT32; sp.out_dtype = dt; sp.has_out = true;
+    sp.op_dtypes = {dt, dt, dt};
+    sp.op_modes = {M_PAIR0, M_PAIR1, M_PAIR1};
+    sp.op_alias = {-1, 0, -1};
+    sp.op_salias = {-1, 0, 0};
+    nvrtc_compile(gen_source(sp, t), a);
+    ++n;
   }
   return n;
 }
