@@ -1584,6 +1584,13 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     std::vector<uint64_t> w;
     fill_common_words(s, sp, tape, L, w);
     w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+    // 32-bit coordinate decoding (magic-number division) when every index fits
+    {
+      bool small = KN * S < (1ll << 31) && RN < (1ll << 31);
+      for (int d = 0; d < s.nd; ++d) if (s.shape[d] >= (1ll << 31)) small = false;
+      if (small) for (int d = 0; d < s.nd; ++d) compute_magic(std::max<int64_t>(s.shape[d], 1), w[L.magic + d]);
+      sp.idx32 = small ? 1 : 0;
+    }
     StreamScratch part(S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0, stream);
     if (S > 1) {
       uint64_t* p = (uint64_t*)part.ptr;
