@@ -546,6 +546,13 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
             e = e * 0.125
         out = nca.NCDevArray((16, 256, 512), nca.DType.float32)
         fn = lambda: e.evaluate(out=out)  # noqa: E731
+    elif op == "binning-reshape":
+        # the same binning as reshape(16, 2, 256, 2, 512, 2).sum((1, 3, 5))
+        data = nca.NCDevArray((32, 512, 1024), nca.DType.float32)
+        data._buf.view(torch.float32).copy_(torch.rand(32 * 512 * 1024, device="cuda"))
+        six = data.reshape(16, 2, 256, 2, 512, 2)._expr()
+        out = nca.NCDevArray((16, 256, 512), nca.DType.float32)
+        fn = lambda: six.evaluate(reductions=[(nca.RedOp.SUM, (1, 3, 5))], red_out=[out])  # noqa: E731
     elif op == "c5-small":
         # the batched reduction on 1,000 of the uneven arrays (about 1 GB)
         from ncarray_gb300.batch import Batch

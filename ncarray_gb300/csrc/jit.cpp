@@ -697,6 +697,8 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
          << "*)p = (" << storage_uint(dtinfo(sdt).size) << ")s; }\n";
       os << "__device__ __forceinline__ double nca_sum_as_double(u64 s) { return (double)(" << (sgn ? "(i64)s" : "s") << "); }\n";
     } else {
+      // a float32 sum of a float-float accumulator rounds hi + lo once, in float32
+      if (sdt == NCA_FLOAT32 && sum_mode == 0) os << "#define NCA_SUM_FF32 1\n";
       if (sdt == NCA_FLOAT32) os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(float*)p = __double2float_rn(s); }\n";
       else os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(double*)p = s; }\n";
       os << "__device__ __forceinline__ double nca_sum_as_double(double s) { return s; }\n";
