@@ -346,6 +346,7 @@ struct Spec {
   // kind 7 (bulk-copy staged): stages, p-row / uniform operand masks, fastest
   // loop dim, number of p-row operands, log2(tp / 8)
   int ns = 0, ld = 0, npc = 0, ltp8 = 3, nmaps = 1;
+  int nob = 2;     // kind 7: output tiles (TMA-store double buffering when 2)
   uint32_t pmask = 0, umask = 0, uumask = 0;
   uint32_t ptrmask = 0;   // operands on a pointer axis (kinds 2, 3, 4)
 };
@@ -547,7 +548,7 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
   if (sp.kind == 6 && sp.minb > 1) os << "#define NCA_LB 256, " << sp.minb << "\n";
   else os << "#define NCA_LB 256\n";
   // kind 7: CTAs per SM its shared memory allows (the register cap follows)
-  if (sp.kind == 7) os << "#define NCA_K7_MINB " << std::max(1, sp.minb) << "\n";
+  if (sp.kind == 7) os << "#define NCA_K7_MINB " << std::max(1, sp.minb) << "\n#define NCA_NOB " << sp.nob << "\n";
   os << "#define NCA_GRP " << sp.grp << "\n";
   os << "#define NCA_QD " << sp.qd << "\n#define NCA_QXP " << sp.qxp << "\n#define NCA_QX " << sp.qx << "\n#define NCA_TP " << sp.tp
      << "\n#define NCA_RB " << sp.rb << "\n#define NCA_TMASK " << sp.tmask << "u\n#define NCA_TILE_BYTES "
@@ -903,6 +904,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
   add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
+  add(sp.nob);
   for (int d : sp.op_dtypes) add(d);
   k += '|';
   for (int m : sp.op_modes) add(m);
@@ -1191,11 +1193,13 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   if (const char* e = getenv("NCA_STAGED_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) rb_max = v; }
   int ns_want = 2;
   if (const char* e = getenv("NCA_STAGED_STAGES")) { const int v = atoi(e); if (v >= 2 && v <= 6) ns_want = v; }
-  // stages, two output tiles, full/empty mbarriers per stage and two per output tile
+  int nob = 2;
+  if (const char* e = getenv("NCA_STAGED_OUTBUFS")) { const int v = atoi(e); if (v == 1 || v == 2) nob = v; }
+  // stages, output tiles, full/empty mbarriers per stage and per output tile
   auto smem_for = [&](int c, int n) {
     const int64_t rq = (int64_t)c * QX;
     const int64_t stage = nt * ((rq / 32) * tp * 128) + npc * (rq * 128);
-    return n * stage + 2 * (rq * 128) + 16 * n + 32 + 1024;
+    return n * stage + nob * (rq * 128) + 16 * n + 16 * nob + 1024;
   };
   int rb = 0, ns = 2;
   for (int c = 16; c >= 1 && rb == 0; c /= 2) {
@@ -1220,6 +1224,7 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   while (qxp < QX) qxp *= 2;
   sp.qd = qd; sp.qx = (int)QX; sp.qxp = qxp; sp.tp = tp; sp.rb = rb; sp.tmask = tmask; sp.tile_bytes = 0;
   sp.ns = ns; sp.ld = ld; sp.npc = npc; sp.pmask = pmask; sp.umask = umask; sp.uumask = uumask; sp.ltp8 = 2;
+  sp.nob = nob;
   sp.nmaps = nt + npc + (sp.has_out ? 1 : 0);
   // as many CTAs per SM as their shared memory allows (228 KiB per SM, 1 KiB
   // reserved per CTA), at most three: ptxas caps the registers to match
@@ -1744,6 +1749,10 @@ int jit_selftest(const char* arch) {
       a7.nd = 5; a7.kept_mask = 1u | 2u | 16u; a7.ld = 3; a7.nred = 2; a7.red_ops = 2u | (4u << 4); a7.has_max = true;
       nvrtc_compile(gen_source(a7, t), a);
       ++n;
+      ++n;
+      // one output tile (three stages fit beside it)
+      a7.nob = 1; a7.ns = 3;
+      nvrtc_compile(gen_source(a7, t), a);
       ++n;
     }
   }
