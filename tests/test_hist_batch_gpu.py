@@ -10,6 +10,7 @@ import pytest
 
 import ncarray_gb300 as nca
 from ncarray_gb300.batch import Batch
+from ncarray_gb300.dtype import DType
 from ncarray_gb300.hist import hist2d
 from tests.helpers import SEED
 
@@ -164,3 +165,69 @@ def test_batch_relative_error_with_cancellation(cuda, orc):
     got = Batch(arrays).run().to_host()
     rel = np.abs(got[:, 0] - ref[:, 0]) / np.abs(ref[:, 0])
     assert rel.max() <= 1e-6, rel.max()
+
+
+def _edge_case_batch(rng, lens, dts, offset_of):
+    """Arrays of the given lengths and dtypes, each a view of a larger device
+    buffer starting offset_of(i) elements in (misaligned bodies, head and tail
+    elements outside the 16-byte aligned part)."""
+    arrays, host, codes = [], [], []
+    for i, (L, dt) in enumerate(zip(lens, dts)):
+        off = offset_of(i)
+        x = (np.exp(rng.normal(0, 2, L + off + 3)) * rng.choice([-1.0, 1.0], L + off + 3)).astype(np.float32)
+        if dt == DType.float32:
+            h = x
+        elif dt == DType.bfloat16:
+            h = (x.view(np.uint32) >> 16).astype(np.uint16)
+        else:
+            h = x.astype(np.float16)
+        big = nca.NCDevArray.from_host(h, dt)
+        arrays.append(big[off:off + L])
+        host.append(np.ascontiguousarray(h[off:off + L]))
+        codes.append(int(dt))
+    return arrays, host, codes
+
+
+def _check_edges(got, ref, host, codes):
+    lowest = float(np.finfo(np.float32).min)
+    for i, x in enumerate(host):
+        if x.size == 0:
+            assert got[i, 0] == 0.0 and np.isnan(got[i, 1]) and got[i, 2] == lowest and got[i, 3] == 0.0, got[i]
+            continue
+        if codes[i] == int(DType.bfloat16):
+            xf = (x.astype(np.uint32) << 16).view(np.float32)
+        else:
+            xf = x.astype(np.float32)
+        scale = float(np.abs(xf.astype(np.float64)).sum())
+        for k in (0, 1, 3):
+            assert abs(got[i, k] - ref[i, k]) <= 1e-6 * abs(ref[i, k]) + 1e-9 * scale, (i, x.size, k, got[i], ref[i])
+        assert got[i, 2] == ref[i, 2], (i, x.size, got[i, 2], ref[i, 2])
+
+
+def test_batch_edges(cuda, orc):
+    """Lengths around every boundary of the pipeline (16-byte vectors, slabs,
+    chunks), empty arrays, all three dtypes, bodies starting 0..7 elements
+    past an aligned address, a batch of arrays shorter than 16 bytes, and a
+    batch of one array."""
+    rng = np.random.default_rng(SEED + 8)
+    base = [0, 1, 2, 3, 4, 5, 7, 8, 9, 15, 16, 17, 31, 33, 63, 65, 127, 129, 4095, 4096, 4097,
+            65535, 65536, 65537, 131071, 131073, 262143, 262145]
+    lens, dts = [], []
+    for dt in (DType.float32, DType.bfloat16, DType.float16):
+        lens += base
+        dts += [dt] * len(base)
+    arrays, host, codes = _edge_case_batch(rng, lens, dts, lambda i: i % 8)
+    ref = orc.batch_reduce(host, codes, nthreads=4)
+    b = Batch(arrays)
+    _check_edges(b.run().to_host(), ref, host, codes)
+    _check_edges(b.run(graph=True).to_host(), ref, host, codes)
+    # only head/tail elements (no 16-byte aligned body)
+    lens = [1, 2, 3, 5, 7] * 6
+    dts = [DType.float32, DType.bfloat16, DType.float16] * 10
+    arrays, host, codes = _edge_case_batch(rng, lens, dts, lambda i: (3 * i) % 8)
+    ref = orc.batch_reduce(host, codes, nthreads=4)
+    _check_edges(Batch(arrays).run().to_host(), ref, host, codes)
+    # one array
+    arrays, host, codes = _edge_case_batch(rng, [1 << 20], [DType.float32], lambda i: 5)
+    ref = orc.batch_reduce(host, codes, nthreads=4)
+    _check_edges(Batch(arrays).run().to_host(), ref, host, codes)
