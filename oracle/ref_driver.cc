@@ -148,7 +148,7 @@ int ref_expr_eval(const uint32_t* instrs, int n_instrs, int n_arrays, void* cons
         case 3: run_vm<3, DestT>(e, result); break;
         case 4: run_vm<4, DestT>(e, result); break;
         case 5: run_vm<5, DestT>(e, result); break;
-        default: throw std::runtime_error("ndim 1..5 supported by the driver");
+        default: throw std::runtime_error("ndim 1..5 supported by ref_driver");
       }
     };
     switch ((DType)expr_dtype) {
@@ -164,7 +164,7 @@ int ref_expr_eval(const uint32_t* instrs, int n_instrs, int n_arrays, void* cons
       case DType::int64: go.operator()<std::int64_t>(); break;
       case DType::float32: go.operator()<float>(); break;
       case DType::float64: go.operator()<double>(); break;
-      default: throw std::runtime_error("expr dtype not supported by the driver");
+      default: throw std::runtime_error("expr dtype not supported by ref_driver");
     }
     return 0;
   } catch (const std::exception& ex) {
@@ -212,7 +212,7 @@ int ref_reduce_axes(void* data, int dtype, int ndim, const int64_t* shape, const
       case 0: r = v.sum(axes); break;
       case 2: r = v.max(axes); break;
       case 3: r = v.min(axes); break;
-      default: throw std::runtime_error("axis op not pinned by the driver");
+      default: throw std::runtime_error("axis op not pinned by ref_driver");
     }
     const int64_t bytes = (int64_t)r.size() * (int64_t)r.itemsize();
     if (bytes > out_cap_bytes) throw std::runtime_error("output buffer too small");

@@ -95,7 +95,7 @@ def main():
     # random tapes over the integer and float dtypes
     binops = [14, 15, 16, 17, 18, 20, 21, 22, 23, 24, 25, 26, 27]
     # LNOT is left out: the reference VM skips it (dynamicmvnode.hh:203-204), a
-    # defect this build does not reproduce (LNOT negates here).
+    # defect the library does not reproduce (LNOT negates here).
     unops = [5, 6, 7]
     for t in range(40):
         dt1 = int(rng.choice([B, U8, U16, U32, U64, I8, I16, I32, I64, F32, F64]))
