@@ -26,6 +26,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <fstream>
 #include <sstream>
 #include <string>
@@ -589,6 +590,14 @@ int32_t nca_batch_create(const nca_batch_item* items, int32_t n_items, nca_batch
       B->items.assign(items, items + n_items);
       B->shape_class = shape_class(B);
       load_tuned(B);
+      // NCA_BATCH_SCHEDULE="<chunk bytes>,<threads>,<slab bytes>,<CTAs per SM>" overrides the tuned schedule
+      if (const char* e = getenv("NCA_BATCH_SCHEDULE")) {
+        long long cb = 0;
+        int th = 0, sl = 0, cps = 0;
+        if (sscanf(e, "%lld,%d,%d,%d", &cb, &th, &sl, &cps) == 4 && schedule_ok(cb, th, sl, cps)) {
+          B->chunk_bytes = cb; B->threads = th; B->slab = sl; B->ctas_per_sm = cps;
+        }
+      }
       build_chunks(B, (cudaStream_t)stream);
     } catch (...) {
       nca_batch_destroy(B);
