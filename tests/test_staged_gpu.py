@@ -1,7 +1,7 @@
 """Fused expressions + reductions whose operands are transposed relative to the
 output, staged through shared memory by the JIT kernel classes 6 (register
-staging, any layout) and 7 (bulk-copy staging of contiguous aligned rows, with
-the ordered merge of class 8), vs the oracle.
+staging, any layout) and 7 (TMA tiles on a warp-specialised pipeline, units
+split between CTAs merged in CTA order), vs the oracle.
 
 Covers partial p tiles, q extents from 2 to 32, two staged operands, float64
 and int32 staged operands, several reduced axes, every reduction op, units
@@ -124,5 +124,32 @@ def test_async_staged_plain_and_argmax_ties(cuda, orc, monkeypatch, async_on):
     yr = oracle_eval(orc, y, [xp])
     assert_bits_equal(out.to_host(), yr, "stored value")
     mx, am = y.evaluate(reductions=[(RedOp.MAX, 2), (RedOp.ARGMAX, 2)])
+    check_reduction(orc, yr, DType.float32, RedOp.MAX, 2, mx.to_host())
+    check_reduction(orc, yr, DType.float32, RedOp.ARGMAX, 2, am.to_host())
+
+
+@pytest.mark.parametrize("rb,stages,outbufs", [("4", "3", "2"), ("8", "3", "1"), ("16", "2", "1"), ("8", "6", "2")])
+@pytest.mark.parametrize("shape", [(8, 16, 32, 64), (16, 6, 48, 96)])
+def test_async_staged_tuning_knobs(cuda, orc, monkeypatch, rb, stages, outbufs, shape):
+    """Class 7 under other blocks of loop indices, pipeline depths and one or
+    two output tiles: the same bits as the oracle for the stored value and
+    max/argmax."""
+    monkeypatch.setenv("NCA_STAGED_ASYNC", "1")
+    monkeypatch.setenv("NCA_STAGED_RB", rb)
+    monkeypatch.setenv("NCA_STAGED_STAGES", stages)
+    monkeypatch.setenv("NCA_STAGED_OUTBUFS", outbufs)
+    rng = np.random.default_rng(SEED + 75)
+    q, b, r, p = shape
+    x = rng.normal(size=(p, b, r, q)).astype(np.float32)
+    xp = x.transpose(3, 1, 2, 0)
+    vv = rng.normal(size=b).astype(np.float32)
+    k = rng.integers(-1000, 1001, xp.shape).astype(np.int32)
+    dx, dv, dk = dev(x).permute(3, 1, 2, 0), dev(vv).reshape(1, b, 1, 1), dev(k)
+    with nca.lazy_mode():
+        y = dx * dv + dk
+    out = nca.NCDevArray(y.shape, y.dtype)
+    mx, am = y.evaluate(out=out, reductions=[(RedOp.MAX, 2), (RedOp.ARGMAX, 2)])
+    yr = oracle_eval(orc, y, [xp, vv.reshape(1, b, 1, 1), k])
+    assert_bits_equal(out.to_host(), yr, "stored value")
     check_reduction(orc, yr, DType.float32, RedOp.MAX, 2, mx.to_host())
     check_reduction(orc, yr, DType.float32, RedOp.ARGMAX, 2, am.to_host())
