@@ -1699,6 +1699,12 @@ int jit_selftest(const char* arch) {
       const std::string src = gen_source(sp, t);
       nvrtc_compile(src, a);
       ++n;
+      if (kind == 3) {   // one thread per kept position (the reduced-offset table)
+        Spec s1 = sp;
+        s1.team = 1;
+        nvrtc_compile(gen_source(s1, t), a);
+        ++n;
+      }
     }
     // kinds 2, 3, 4 with operand 0 on a pointer axis (first two dtype rows)
     if (&d - &dts[0] < 2) {
