@@ -1606,7 +1606,9 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
     }
     CUfunction fn = kernel_for(sp, tape);
-    launch(fn, cdiv(KN * S, tpb), w, stream);
+    // one-thread teams stride over their units (a few blocks per SM build the
+    // reduced-offset table once each); wider teams take one unit each
+    launch(fn, sp.team == 1 ? std::min<int64_t>(cdiv(KN * S, tpb), (int64_t)sms * 8) : cdiv(KN * S, tpb), w, stream);
     if (S > 1) {
       Spec fs = sp; fs.kind = 5;
       CUfunction ff = kernel_for(fs, tape);
