@@ -221,7 +221,8 @@ int32_t nca_stencil3d_iterate(const nca_view* a, const nca_view* b, const double
  * iy = floor((y_i - y_lo) * sy) evaluated in float32 with sx = (float)(nbx/(x_hi-x_lo)),
  * sy likewise; points with ix or iy outside [0, nb) are dropped.
  * counts[iy*nbx + ix] += 1 (uint64, exact) and, when w != NULL,
- * wsum[iy*nbx + ix] += w_i (float32 output, accumulated in float64).
+ * wsum[iy*nbx + ix] += w_i (float32 output; compensated float32 partial sums,
+ * their rounding errors collected exactly, combined in float64).
  * counts/wsum are ACCUMULATED into (zero them first for a fresh histogram).
  * Stands in for the scatter_add primitive (kernels.cuh:660-680;
  * host/elementwise.hh:482-505), which has no public API in the reference. */
@@ -265,7 +266,8 @@ int32_t nca_batch_reduce_plain(nca_batch* batch, nca_batch_result* results, void
 /* Times candidate schedules on `stream` and stores the best for this batch's
  * shape class in the autotuner cache (file under the JIT cache directory). */
 int32_t nca_batch_autotune(nca_batch* batch, nca_batch_result* results, void* stream);
-/* Reports the schedule in use: chunk elements, threads per block, items per thread, CTAs. */
+/* Reports the schedule in use: chunk bytes, consumer threads per block, 16-byte
+ * vectors per thread per slab, CTAs. */
 int32_t nca_batch_schedule(const nca_batch* batch, int64_t* chunk, int32_t* threads,
                            int32_t* items_per_thread, int32_t* ctas);
 /* Status word of the last launch (0 = ok, nonzero = a bounded wait gave up). */
