@@ -605,15 +605,29 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
       const int vb = es * sp.vec;
       const int lead = (k < (int)sp.op_alias.size() && sp.op_alias[k] >= 0) ? sp.op_alias[k] : k;
       const std::string wn = "pw" + std::to_string(lead);
-      if (lead == k) {
-        const std::string vt = vec_type(vb);
+      // a pointer operand's panels may sit anywhere: its window is used only when
+      // the panel address is on the vector grid, else scalar loads
+      const bool guarded = ((sp.ptrmask >> lead) & 1u) != 0;
+      const std::string vt = vec_type(vb);
+      if (lead == k && !guarded) {
         g << "  const " << vt << " " << wn << "_0 = *(const " << vt << "*)(" << base << " - " << ph * es << ");\n";
         g << "  const " << vt << " " << wn << "_1 = *(const " << vt << "*)(" << base << " + " << vb - ph * es << ");\n";
+      } else if (lead == k) {
+        g << "  const bool " << wn << "_ok = ((((u64)(" << base << ")) - " << ph * es << ") & " << vb - 1 << ") == 0;\n";
+        g << "  " << vt << " " << wn << "_0 = {}, " << wn << "_1 = {};\n";
+        g << "  if (" << wn << "_ok) { " << wn << "_0 = *(const " << vt << "*)(" << base << " - " << ph * es << "); "
+          << wn << "_1 = *(const " << vt << "*)(" << base << " + " << vb - ph * es << "); }\n";
       }
       for (int q = 0; q < sp.vec; ++q) {
         const int j = ph + 2 * q;
-        g << "  v[" << k << "][" << q << "] = (nca_w)("
-          << from_bits(dt, lane_bits(vb, es, j % sp.vec, wn + "_" + std::to_string(j / sp.vec))) << ");\n";
+        const std::string lanev = "(nca_w)(" + from_bits(dt, lane_bits(vb, es, j % sp.vec, wn + "_" + std::to_string(j / sp.vec))) + ")";
+        if (!guarded) {
+          g << "  v[" << k << "][" << q << "] = " << lanev << ";\n";
+        } else {
+          g << "  v[" << k << "][" << q << "] = " << wn << "_ok ? " << lanev << " : "
+            << scalar_load(k, base + " + " + std::to_string(q) + " * OPS_(" + std::to_string(k) + ", " + std::to_string(sp.nd - 1) + ")")
+            << ";\n";
+        }
       }
     } else {
       for (int q = 0; q < sp.vec; ++q)
@@ -995,17 +1009,23 @@ static void plan_pairs(const Space& s, Spec& sp) {
   sp.op_alias.assign(sp.nops, -1);
   const int ax = s.nd - 1;
   if (sp.vec < 2) return;
-  auto window = [&](int k) {
-    const int64_t es = dtinfo(s.ops[k].dtype).size;
-    return (uintptr_t)s.ops[k].base - (uintptr_t)(sp.op_modes[k] == M_PAIR1 ? es : 0);
+  // the window start of operand k in its own terms: the base (or, on a pointer
+  // axis, the panel offset) minus the phase
+  auto wstart = [&](int k) {
+    const CArr& a = s.ops[k];
+    const int64_t es = dtinfo(a.dtype).size, ph = sp.op_modes[k] == M_PAIR1 ? es : 0;
+    return a.ptr ? (int64_t)a.ptc - ph : (int64_t)((uintptr_t)a.base - (uintptr_t)ph);
   };
   for (int k = 0; k < sp.nops; ++k) {
     if (sp.op_modes[k] != M_STRIDED) continue;
     const CArr& a = s.ops[k];
-    if (a.ptr) continue;
     const int64_t es = dtinfo(a.dtype).size, vb = es * sp.vec;
     if ((vb != 8 && vb != 16) || a.st[ax] != 2 * es) continue;
-    const int64_t ph = (int64_t)((uintptr_t)a.base % (uintptr_t)vb);
+    // pointer operands: the table must not move along the vector axis; the
+    // panels' own alignment is checked by the kernel (scalar loads otherwise)
+    if (a.ptr && a.pts[ax] != 0) continue;
+    const uintptr_t start = a.ptr ? (uintptr_t)a.ptc : (uintptr_t)a.base;
+    const int64_t ph = (int64_t)(start % (uintptr_t)vb);
     if (ph != 0 && ph != es) continue;
     bool ok = true;
     for (int d = 0; d < ax && ok; ++d) if (a.st[d] % vb != 0) ok = false;
@@ -1013,9 +1033,14 @@ static void plan_pairs(const Space& s, Spec& sp) {
     sp.op_modes[k] = ph == 0 ? M_PAIR0 : M_PAIR1;
     for (int j = 0; j < k; ++j) {
       if ((sp.op_modes[j] != M_PAIR0 && sp.op_modes[j] != M_PAIR1) || sp.op_alias[j] >= 0) continue;
-      if (dtinfo(s.ops[j].dtype).size != es || window(j) != window(k)) continue;
+      const CArr& o = s.ops[j];
+      if (dtinfo(o.dtype).size != es || o.ptr != a.ptr || wstart(j) != wstart(k)) continue;
       bool same = true;
-      for (int d = 0; d <= ax; ++d) if (s.ops[j].st[d] != a.st[d]) same = false;
+      for (int d = 0; d <= ax; ++d) if (o.st[d] != a.st[d]) same = false;
+      if (a.ptr) {
+        if (o.table != a.table) same = false;
+        for (int d = 0; d <= ax; ++d) if (o.pts[d] != a.pts[d]) same = false;
+      }
       if (same) { sp.op_alias[k] = j; break; }
     }
   }
@@ -1774,6 +1799,11 @@ int jit_selftest(const char* arch) {
     sp.op_modes = {M_PAIR0, M_PAIR1, M_PAIR1};
     sp.op_alias = {-1, 0, -1};
     sp.op_salias = {-1, 0, 0};
+    nvrtc_compile(gen_source(sp, t), a);
+    ++n;
+    // the same with operands 0 and 1 on a pointer axis (windows guarded per panel)
+    sp.ptrmask = 3u;
+    sp.op_salias = {-1, -1, -1};
     nvrtc_compile(gen_source(sp, t), a);
     ++n;
   }

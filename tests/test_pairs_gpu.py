@@ -106,3 +106,34 @@ def test_binning_pairs(cuda, orc, bins):
                     e = v if e is None else e + v
         e = e * (1.0 / (bp * br * bc))
     run(e, pairs, orc, f"binning {bins}")
+
+
+@pytest.mark.parametrize("layout", ["aligned", "offset", "alternating"])
+def test_binning_pairs_on_panels(cuda, orc, layout):
+    """The binning views on a table of panels (pointer axis): window loads
+    where a panel is on the 16-byte grid, scalar loads where it is not
+    (panels starting one element in), chosen per panel at run time."""
+    rng = np.random.default_rng(SEED + 154)
+    P, R, C = 8, 32, 128
+    h = rand(rng, (P, R, C), DType.float32)
+    if layout == "aligned":
+        panels = [nca.NCDevArray.from_host(h[i]) for i in range(P)]
+    else:
+        # rows of C + 4 elements (16-byte multiples); a panel starts 0 or 1 element in
+        big = np.zeros((P, R, C + 4), np.float32)
+        starts = [1] * P if layout == "offset" else [i % 2 for i in range(P)]
+        for i in range(P):
+            big[i, :, starts[i]:starts[i] + C] = h[i]
+        dbig = nca.NCDevArray.from_host(big)
+        panels = [dbig[i][:, starts[i]:starts[i] + C] for i in range(P)]
+    T = nca.NCDevArray.from_panels(panels)
+    pairs, e = [], None
+    with nca.lazy_mode():
+        for p in range(2):
+            for r_ in range(2):
+                for c_ in range(2):
+                    v = T[p::2, r_::2, c_::2]
+                    pairs.append((v, h[p::2, r_::2, c_::2]))
+                    e = v if e is None else e + v
+        e = e * 0.125
+    run(e, pairs, orc, f"panels {layout}")
