@@ -543,6 +543,16 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
     sum_mode = ra == NCA_FLOAT32 ? 0 : ra == NCA_FLOAT64 ? 1 : 2;
   }
   os << "#define NCA_SUM_MODE " << sum_mode << "\n";
+  // extremes keep an index only when an argmax (op 4) / argmin (op 5) is asked for
+  {
+    bool mxi = false, mni = false;
+    for (int k = 0; k < sp.nred; ++k) {
+      const int op = (int)((sp.red_ops >> (4 * k)) & 15u);
+      if (op == 4) mxi = true;
+      if (op == 5) mni = true;
+    }
+    os << "#define NCA_MX_IDX " << (mxi ? 1 : 0) << "\n#define NCA_MN_IDX " << (mni ? 1 : 0) << "\n";
+  }
   os << "#define NCA_UNROLL " << sp.unroll << "\n#define NCA_KNAME " << kernel_name(sp.kind) << "\n";
   // the staged class asks for sp.minb resident CTAs per SM (register cap)
   if (sp.kind == 6 && sp.minb > 1) os << "#define NCA_LB 256, " << sp.minb << "\n";
@@ -714,9 +724,18 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
     } else {
       // a float32 sum of a float-float accumulator rounds hi + lo once, in float32
       if (sdt == NCA_FLOAT32 && sum_mode == 0) os << "#define NCA_SUM_FF32 1\n";
-      if (sdt == NCA_FLOAT32) os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(float*)p = __double2float_rn(s); }\n";
-      else os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(double*)p = s; }\n";
-      os << "__device__ __forceinline__ double nca_sum_as_double(double s) { return s; }\n";
+      if (sum_mode == 0) {
+        os << "struct NcaFF { float hi, lo; };   // float-float partial sum\n";
+        if (sdt == NCA_FLOAT32)
+          os << "__device__ __forceinline__ void nca_store_sum(char* p, NcaFF s) { *(float*)p = __fadd_rn(s.hi, s.lo); }\n";
+        else
+          os << "__device__ __forceinline__ void nca_store_sum(char* p, NcaFF s) { *(double*)p = __dadd_rn((double)s.hi, (double)s.lo); }\n";
+        os << "__device__ __forceinline__ double nca_sum_as_double(NcaFF s) { return __dadd_rn((double)s.hi, (double)s.lo); }\n";
+      } else {
+        if (sdt == NCA_FLOAT32) os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(float*)p = __double2float_rn(s); }\n";
+        else os << "__device__ __forceinline__ void nca_store_sum(char* p, double s) { *(double*)p = s; }\n";
+        os << "__device__ __forceinline__ double nca_sum_as_double(double s) { return s; }\n";
+      }
     }
   }
   os << "#undef OPB_\n#undef OPS_\n";
@@ -1154,6 +1173,17 @@ static int find_staged(const Space& s, uint32_t& tmask, int& nt) {
 // Kind 7: the staged shape with 4-byte elements whose tiles TMA can move (see
 // the template). Returns false, launching nothing, when the views do not
 // allow it.
+// the finalize pass: a warp per kept position when there are few (global
+// reductions), a thread per kept position when there are many
+static void launch_finalize(const Spec& sp, const Tape& tape, int64_t KN, int sms, std::vector<uint64_t>& w,
+                            cudaStream_t stream) {
+  Spec fs = sp;
+  fs.kind = 5;
+  fs.team = KN >= 32768 ? 1 : 32;
+  CUfunction ff = kernel_for(fs, tape);
+  launch(ff, std::min<int64_t>(cdiv(KN, fs.team == 1 ? 256 : 8), (int64_t)sms * 8), w, stream);
+}
+
 static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int qd, uint32_t tmask, int nt, int64_t KN,
                                 int64_t RN, cudaStream_t stream) {
   // NCA_STAGED_ASYNC=0 keeps these views on kind 6 (read on every call)
@@ -1416,10 +1446,7 @@ static void launch_staged(const Space& s, Spec sp, const Tape& tape, int qd, uin
   }
   launch(fn, units * S, w, stream, smem);
   if (split) {
-    Spec fs = sp;
-    fs.kind = 5;
-    CUfunction ff = kernel_for(fs, tape);
-    launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
+    launch_finalize(sp, tape, KN, sms, w, stream);
   }
 }
 
@@ -1599,10 +1626,13 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     if (RN > 0) plan_vec(s, sp, 16, false); else { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
     if (sp.vec > 1 && s.shape[s.nd - 1] % sp.vec != 0) { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
     // team of threads per kept position: a block for long reductions, a warp
-    // for medium ones, one thread when fewer than 64 elements are reduced
-    sp.team = RN >= 4096 ? 256 : (RN >= 64 ? 32 : 1);
+    // for medium ones, one thread for short ones (below 64 elements, or below
+    // 1024 along a single reduced dim, where a warp's shuffle tree would cost
+    // more than its row)
+    const int64_t team1_max = s.nd - sp.nkept == 1 ? 1024 : 64;
+    sp.team = RN >= 4096 ? 256 : (RN >= team1_max ? 32 : 1);
     const int64_t tpb = 256 / sp.team;
-    const int64_t target = (int64_t)sms * tpb * 4;
+    const int64_t target = (int64_t)sms * tpb * 8;
     int64_t S = 1;
     if (KN < target && RN > 0) {
       S = cdiv(target, KN);
@@ -1635,9 +1665,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     // reduced-offset table once each); wider teams take one unit each
     launch(fn, sp.team == 1 ? std::min<int64_t>(cdiv(KN * S, tpb), (int64_t)sms * 8) : cdiv(KN * S, tpb), w, stream);
     if (S > 1) {
-      Spec fs = sp; fs.kind = 5;
-      CUfunction ff = kernel_for(fs, tape);
-      launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
+      launch_finalize(sp, tape, KN, sms, w, stream);
     }
     return;
   }
@@ -1677,9 +1705,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   CUfunction fn = kernel_for(sp, tape);
   launch(fn, cdiv(KG * S, 256), w, stream);
   if (S > 1) {
-    Spec fs = sp; fs.kind = 5;
-    CUfunction ff = kernel_for(fs, tape);
-    launch(ff, std::min<int64_t>(cdiv(KN, 256), (int64_t)sms * 8), w, stream);
+    launch_finalize(sp, tape, KN, sms, w, stream);
   }
 }
 
@@ -1726,7 +1752,7 @@ int jit_selftest(const char* arch) {
       const std::string src = gen_source(sp, t);
       nvrtc_compile(src, a);
       ++n;
-      if (kind == 3) {   // one thread per kept position (the reduced-offset table)
+      if (kind == 3 || kind == 5) {   // one thread per kept position (offset table; thread-per-position finalize)
         Spec s1 = sp;
         s1.team = 1;
         nvrtc_compile(gen_source(s1, t), a);
