@@ -443,6 +443,49 @@ def measure_binning(torch, nca, peak, flush_buf, reps=20):
     return res
 
 
+def measure_reductions(torch, nca, peak, reps=50):
+    """Plain axis and global reductions of 256 MB float32 arrays (inputs larger
+    than L2; CUDA-graph replays of one evaluate call each): the reduction
+    kinds on their own, checked against numpy on the host."""
+    cases = [
+        ("global_sum", (64 << 20,), [(nca.RedOp.SUM, None)]),
+        ("global_max", (64 << 20,), [(nca.RedOp.MAX, None)]),
+        ("sum_last_axis_4096x16384", (4096, 16384), [(nca.RedOp.SUM, 1)]),
+        ("sum_last_axis_1Mx64", (1 << 20, 64), [(nca.RedOp.SUM, 1)]),
+        ("sum_axis0_4096x16384", (4096, 16384), [(nca.RedOp.SUM, 0)]),
+        ("max_axis1_256x256x1024", (256, 256, 1024), [(nca.RedOp.MAX, 1)]),
+        ("argmax_last_axis_4096x16384", (4096, 16384), [(nca.RedOp.ARGMAX, 1)]),
+    ]
+    res = {}
+    gen = torch.Generator(device="cuda").manual_seed(SEED + 9)
+    for name, shape, red in cases:
+        x = torch.randn(int(np.prod(shape)), device="cuda", dtype=torch.float32, generator=gen)
+        d = nca.NCDevArray(shape, nca.DType.float32, _buf=x.view(torch.uint8))
+        e = d._expr()
+        outs = e.evaluate(reductions=red)
+        g = make_graph(torch, lambda: e.evaluate(reductions=red))
+        for _ in range(3):
+            g.replay()
+        ms = time_events(torch, g.replay, reps)
+        nbytes = x.numel() * 4
+        op, axes = red[0]
+        xh = x.view(shape).cpu().numpy()
+        got = outs[0].to_host()
+        if op == nca.RedOp.SUM:
+            want = xh.astype(np.float64).sum(axis=axes)
+            ok = bool(np.all(np.abs(got - want) <= 1e-6 * np.abs(xh).astype(np.float64).sum(axis=axes) + 1e-30))
+        elif op == nca.RedOp.MAX:
+            ok = bool(np.array_equal(got, xh.max(axis=axes)))
+        else:
+            ok = bool(np.array_equal(got, xh.argmax(axis=axes)))
+        res[name] = {"GB/s": round(nbytes / ms / 1e6, 1), "frac_of_measured": round(nbytes / ms / 1e6 / peak, 4),
+                     "us": round(ms * 1e3, 2), "matches_numpy": ok}
+        del x, d, e, g, outs
+        torch.cuda.empty_cache()
+    res["l2"] = "inputs 256 MB > L2; no flush"
+    return res
+
+
 def c5_arrays(torch, nca, n_arrays):
     """n_arrays 1-D device arrays with lengths log-uniform in [64, 2^22],
     alternately float32 and bfloat16, x = exp(N(0, 2)) with random signs,
@@ -645,7 +688,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--headline-only", action="store_true", help="skip the per-op measurements of the other workloads")
-    ap.add_argument("--only", default=None, choices=["c1", "c3", "c4", "c5", "binning"],
+    ap.add_argument("--only", default=None, choices=["c1", "c3", "c4", "c5", "binning", "reductions"],
                     help="measure one per-op workload and print its figures (no headline line)")
     ap.add_argument("--profile-op", default=None, help="run one op --steps times for a profiler capture")
     args = ap.parse_args()
@@ -664,7 +707,8 @@ def main():
         flush_buf = torch.empty(512 << 20, dtype=torch.uint8, device="cuda") if args.only in ("c1", "binning") else None
         fn = {"c1": lambda: measure_c1(torch, nca, peak, flush_buf), "c3": lambda: measure_c3(torch, nca, peak),
               "c4": lambda: measure_c4(torch, nca, peak), "c5": lambda: measure_c5(torch, nca, peak),
-              "binning": lambda: measure_binning(torch, nca, peak, flush_buf)}[args.only]
+              "binning": lambda: measure_binning(torch, nca, peak, flush_buf),
+              "reductions": lambda: measure_reductions(torch, nca, peak)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
         return
 
@@ -900,7 +944,8 @@ def main():
                          ("c3_stencil_f32", lambda: measure_c3(torch, nca, peak)),
                          ("c4_hist2d", lambda: measure_c4(torch, nca, peak)),
                          ("c5_batched", lambda: measure_c5(torch, nca, peak)),
-                         ("binning", lambda: measure_binning(torch, nca, peak, flush_buf))):
+                         ("binning", lambda: measure_binning(torch, nca, peak, flush_buf)),
+                         ("reductions", lambda: measure_reductions(torch, nca, peak))):
             try:
                 per_op[name] = fn()
             except Exception as ex:  # a failed side measurement must not hide the headline
