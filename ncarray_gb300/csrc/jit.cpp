@@ -1626,11 +1626,12 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     if (RN > 0) plan_vec(s, sp, 16, false); else { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
     if (sp.vec > 1 && s.shape[s.nd - 1] % sp.vec != 0) { sp.vec = 1; sp.op_modes.assign(nops, M_STRIDED); }
     // team of threads per kept position: a block for long reductions, a warp
-    // for medium ones, one thread for short ones (below 64 elements, or below
-    // 1024 along a single reduced dim, where a warp's shuffle tree would cost
-    // more than its row)
-    const int64_t team1_max = s.nd - sp.nkept == 1 ? 1024 : 64;
-    sp.team = RN >= 4096 ? 256 : (RN >= team1_max ? 32 : 1);
+    // for medium ones; along one reduced dim, two threads below 1024 elements
+    // (whole sectors per load, where one thread per row uses half of each, and
+    // no warp-wide tree) and one thread up to 8; over several reduced dims, one
+    // thread below 64 elements (its offsets from a per-block table)
+    if (s.nd - sp.nkept == 1) sp.team = RN >= 4096 ? 256 : (RN >= 1024 ? 32 : (RN > 8 ? 2 : 1));
+    else sp.team = RN >= 4096 ? 256 : (RN >= 64 ? 32 : 1);
     const int64_t tpb = 256 / sp.team;
     const int64_t target = (int64_t)sms * tpb * 8;
     int64_t S = 1;
@@ -1661,9 +1662,12 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
     }
     CUfunction fn = kernel_for(sp, tape);
-    // one-thread teams stride over their units (a few blocks per SM build the
-    // reduced-offset table once each); wider teams take one unit each
-    launch(fn, sp.team == 1 ? std::min<int64_t>(cdiv(KN * S, tpb), (int64_t)sms * 8) : cdiv(KN * S, tpb), w, stream);
+    // warp and smaller teams stride over their units from a few blocks per SM
+    // (one-thread teams build their reduced-offset table once per block); a
+    // block team takes one unit per block, so one block's tree and store
+    // overlap the other blocks' loads
+    const int64_t groups = cdiv(KN * S, tpb);
+    launch(fn, sp.team == 256 ? groups : std::min<int64_t>(groups, (int64_t)sms * 8), w, stream);
     if (S > 1) {
       launch_finalize(sp, tape, KN, sms, w, stream);
     }
@@ -1756,6 +1760,12 @@ int jit_selftest(const char* arch) {
         Spec s1 = sp;
         s1.team = 1;
         nvrtc_compile(gen_source(s1, t), a);
+        ++n;
+      }
+      if (kind == 3) {   // two-thread teams (shuffle tree within the team)
+        Spec s2 = sp;
+        s2.team = 2;
+        nvrtc_compile(gen_source(s2, t), a);
         ++n;
       }
     }
