@@ -616,6 +616,13 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
         six = data.reshape(16, 2, 256, 2, 512, 2)._expr()
         out = nca.NCDevArray((16, 256, 512), nca.DType.float32)
         fn = lambda: six.evaluate(reductions=[(nca.RedOp.SUM, (1, 3, 5))], red_out=[out])  # noqa: E731
+    elif op in ("red-global-sum", "red-rows64"):
+        # plain reductions of 256 MB float32: a global sum, a sum over rows of 64
+        shape, red = ((64 << 20,), [(nca.RedOp.SUM, None)]) if op == "red-global-sum" else \
+            ((1 << 20, 64), [(nca.RedOp.SUM, 1)])
+        x = torch.randn(int(np.prod(shape)), device="cuda", dtype=torch.float32)
+        e = nca.NCDevArray(shape, nca.DType.float32, _buf=x.view(torch.uint8))._expr()
+        fn = lambda: e.evaluate(reductions=red)  # noqa: E731
     elif op == "c5-small":
         # the batched reduction on 1,000 of the uneven arrays (about 1 GB)
         from ncarray_gb300.batch import Batch
