@@ -1173,15 +1173,17 @@ static int find_staged(const Space& s, uint32_t& tmask, int& nt) {
 // Kind 7: the staged shape with 4-byte elements whose tiles TMA can move (see
 // the template). Returns false, launching nothing, when the views do not
 // allow it.
-// the finalize pass: a warp per kept position when there are few (global
-// reductions), a thread per kept position when there are many
+// the finalize pass: a block per kept position when there are very few (global
+// reductions), a warp per kept position when there are few, a thread per kept
+// position when there are many
 static void launch_finalize(const Spec& sp, const Tape& tape, int64_t KN, int sms, std::vector<uint64_t>& w,
                             cudaStream_t stream) {
   Spec fs = sp;
   fs.kind = 5;
-  fs.team = KN >= 32768 ? 1 : 32;
+  fs.team = KN >= 32768 ? 1 : (KN <= 64 ? 256 : 32);
   CUfunction ff = kernel_for(fs, tape);
-  launch(ff, std::min<int64_t>(cdiv(KN, fs.team == 1 ? 256 : 8), (int64_t)sms * 8), w, stream);
+  const int64_t per_block = fs.team == 1 ? 256 : (fs.team == 32 ? 8 : 1);   // kept positions per block
+  launch(ff, std::min<int64_t>(cdiv(KN, per_block), (int64_t)sms * 8), w, stream);
 }
 
 static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int qd, uint32_t tmask, int nt, int64_t KN,
@@ -1762,9 +1764,9 @@ int jit_selftest(const char* arch) {
         nvrtc_compile(gen_source(s1, t), a);
         ++n;
       }
-      if (kind == 3) {   // two-thread teams (shuffle tree within the team)
+      if (kind == 3 || kind == 5) {   // two-thread teams; the warp-per-position finalize
         Spec s2 = sp;
-        s2.team = 2;
+        s2.team = kind == 3 ? 2 : 32;
         nvrtc_compile(gen_source(s2, t), a);
         ++n;
       }
