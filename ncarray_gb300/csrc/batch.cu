@@ -182,7 +182,6 @@ constexpr int NSLAB = 4;
 constexpr unsigned long long kWaitNs = 2000000000ull;
 
 
-using nca_dev::gtimer;
 using nca_dev::mbar_wait;
 
 // the 16-byte aligned body of a chunk (computed on the host)

@@ -171,7 +171,6 @@ tile_plan_kernel(const unsigned* __restrict__ est, int nv, long long* __restrict
 // on a timeout the CTA records NCA_ERR_TIMEOUT, waits for its copies in
 // flight and stops. CTA c appends to sub-bucket c % NSUB of every tile.
 
-using nca_dev::gtimer;
 using nca_dev::mbar_wait;
 
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {

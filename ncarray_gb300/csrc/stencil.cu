@@ -46,7 +46,6 @@ template <class T> __host__ __device__ constexpr int stage_bytes() {
 }
 
 
-using nca_dev::gtimer;
 using nca_dev::mbar_wait;
 
 template <class T>
