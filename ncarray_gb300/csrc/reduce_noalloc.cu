@@ -92,8 +92,11 @@ struct Acc {
       if constexpr (sizeof(T) == 4 && T(0.5) != T(0)) {
         const float s = __fadd_rn(hi, x);
         const float bb = __fsub_rn(s, hi);
-        lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb)));
+        const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
         hi = s;
+        // an infinite or NaN running sum has no rounding error to keep
+        // (inf - inf would turn lo, and with it the result, into NaN)
+        lo = fabsf(s) < __int_as_float(0x7f800000) ? __fadd_rn(lo, err) : lo;
       } else if constexpr (T(0.5) != T(0)) {
         d = __dadd_rn(d, x);
       } else {
@@ -291,6 +294,7 @@ extern "C" int32_t nca_reduce_noalloc(const nca_view* src, int32_t op, const nca
     if (n > 0 && !src->data) fail(NCA_ERR_INVALID, "null input data");
     const int odt = out_dtype_for(op, dt);
     if (out->dtype != odt) fail(NCA_ERR_DTYPE, "output dtype %d, expected %s", out->dtype, dtinfo(odt).name);
+    if (out->ndim < 0 || out->ndim > NCA_MAX_NDIM) fail(NCA_ERR_LIMIT, "output ndim %d", out->ndim);
     long long on = 1;
     for (int d = 0; d < out->ndim; ++d) on *= out->shape[d];
     if (on != 1 || !out->data) fail(NCA_ERR_SHAPE, "output must be one element");

@@ -10,7 +10,6 @@ package, and only as the oracle (never as the thing measured or shipped).
 from __future__ import annotations
 
 import ctypes
-import os
 import subprocess
 from ctypes import POINTER, c_double, c_float, c_int, c_int32, c_int64, c_uint32, c_uint64, c_void_p
 from pathlib import Path
@@ -21,7 +20,6 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_LIB = HERE / "_ref" / "libncref.so"
-REF_SRC = Path(os.environ.get("NCA_REFERENCE_DIR", "/root/reference"))
 
 ITEMSIZE = {0: 1, 1: 1, 2: 1, 3: 2, 4: 4, 5: 8, 6: 1, 7: 2, 8: 4, 9: 8, 10: 4, 11: 8, 22: 2, 23: 2}
 
@@ -42,12 +40,14 @@ class OrcResult(ctypes.Structure):
 
 
 def build(with_ref: Optional[bool] = None) -> None:
-    """Builds liboracle.so, and libncref.so when the reference sources exist."""
+    """Builds liboracle.so, and libncref.so when the reference sources exist
+    (their location is the Makefile's REF, or NCA_REFERENCE_DIR)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
     if with_ref is None:
-        with_ref = (REF_SRC / "src" / "lib" / "ncarray").is_dir()
+        with_ref = subprocess.run(["make", "-s", "-C", str(HERE), "have-ref"],
+                                  capture_output=True).returncode == 0
     if with_ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_SRC}"], check=True)
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
 
 
 _orc = None
@@ -67,6 +67,7 @@ def lib() -> ctypes.CDLL:
         L.orc_hist2d.argtypes = [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int, c_double, c_double, c_double,
                                  c_double, c_void_p, c_void_p]
         L.orc_batch_reduce.argtypes = [POINTER(OrcItem), c_int, POINTER(OrcResult), c_int]
+        L.orc_scatter_add.argtypes = [POINTER(OrcView), POINTER(OrcView), POINTER(OrcView)]
         _orc = L
     return _orc
 
@@ -183,6 +184,17 @@ def batch_reduce(arrays: Sequence[np.ndarray], dtypes: Sequence[int], nthreads: 
     return np.array([[r.sum, r.mean, r.max, r.sum_sq_m] for r in res], dtype=np.float64)
 
 
+def scatter_add(dest: np.ndarray, dest_dtype: int, idx: np.ndarray, idx_dtype: int, src: np.ndarray,
+                src_dtype: int) -> np.ndarray:
+    """dest (1-D, updated in place and returned) += src scattered by idx, in
+    the reference's order and arithmetic (host::scatter_add_recursive)."""
+    rc = lib().orc_scatter_add(ctypes.byref(view_of(dest, dest_dtype)), ctypes.byref(view_of(idx, idx_dtype)),
+                               ctypes.byref(view_of(src, src_dtype)))
+    if rc:
+        raise RuntimeError(f"oracle scatter_add failed ({rc})")
+    return dest
+
+
 # ---- the reference's own implementation (oracle/_ref) -------------------------------
 def ref_expr_eval(instrs, scalars, work_dtype: int, expr_dtype: int, operands, out_shape):
     L = ref()
@@ -244,3 +256,22 @@ def ref_reduce_axes(a: np.ndarray, dtype: int, op: int, axes):
     kept = [a.shape[d] for d in range(a.ndim) if not (mask >> d) & 1]
     nbytes = on.value * ITEMSIZE[odt.value]
     return np.frombuffer(bytes(buf)[:nbytes], dtype=np_dtype(odt.value)).reshape(kept), odt.value
+
+
+def ref_scatter_add(dest: np.ndarray, dest_dtype: int, idx: np.ndarray, idx_dtype: int, src: np.ndarray,
+                    src_dtype: int):
+    """dest += src scattered by idx through the reference's own
+    host::scatter_add_recursive; None where oracle/_ref was not built."""
+    L = ref()
+    if L is None:
+        return None
+    n = src.ndim
+    sh = (c_int64 * max(n, 1))(*src.shape)
+    ist = (c_int64 * max(n, 1))(*idx.strides)
+    sst = (c_int64 * max(n, 1))(*src.strides)
+    rc = L.ref_scatter_add(c_void_p(dest.ctypes.data), dest_dtype, c_int64(dest.shape[0]), c_int64(dest.strides[0]),
+                           c_void_p(idx.ctypes.data), idx_dtype, c_void_p(src.ctypes.data), src_dtype, n, sh, ist,
+                           sst)
+    if rc:
+        raise RuntimeError(L.ref_last_error().decode())
+    return dest

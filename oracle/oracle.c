@@ -524,6 +524,46 @@ int orc_stencil3d_f64(double* u, int64_t nz, int64_t ny, int64_t nx, const doubl
   return 0;
 }
 
+/* ---- scatter-add ------------------------------------------------------------------
+ * host::scatter_add_recursive (src/lib/ncarray/host/elementwise.hh:482-505, walking
+ * impl::scatter_reduce_recursive, :33-68): idx and src (equal shapes) are walked in C
+ * index order; an index i with 0 <= i < dest->shape[0] adds the src value, cast to the
+ * dest dtype (op_traits::cast), to dest[i] in the dest dtype (integers wrap, floats
+ * round after every addition). dest is 1-D. Index dtypes are read as int64 (uint64
+ * values >= 2^63 are out of range either way). */
+int orc_scatter_add(const orc_view* dest, const orc_view* idx, const orc_view* src) {
+  if (dest->ndim != 1 || idx->ndim != src->ndim) return 1;
+  const int n = src->ndim;
+  int64_t total = 1;
+  for (int d = 0; d < n; ++d) {
+    if (idx->shape[d] != src->shape[d]) return 2;
+    total *= src->shape[d];
+  }
+  char* db = vbase(dest);
+  const char* ib = vbase(idx);
+  const char* sb = vbase(src);
+  const int64_t dn = dest->shape[0];
+  int64_t c[ORC_MAXD] = {0};
+  for (int64_t e = 0; e < total; ++e) {
+    int64_t rem = e;
+    for (int d = n - 1; d >= 0; --d) { c[d] = rem % src->shape[d]; rem /= src->shape[d]; }
+    const char* pi = ib;
+    const char* ps = sb;
+    for (int d = 0; d < n; ++d) { pi += c[d] * idx->strides[d]; ps += c[d] * src->strides[d]; }
+    const int64_t t = ld_i64(idx->dtype, pi);
+    if (t < 0 || t >= dn) continue;
+    char* pd = db + t * dest->strides[0];
+    switch (dest->dtype) {
+      case D_I32: case D_U32: *(u32*)pd = (u32)(*(u32*)pd + (u32)ld_i64(src->dtype, ps)); break;
+      case D_I64: case D_U64: *(u64*)pd = *(u64*)pd + (u64)ld_i64(src->dtype, ps); break;
+      case D_F32: *(f32*)pd = *(f32*)pd + ld_f32(src->dtype, ps); break;
+      case D_F64: *(f64*)pd = *(f64*)pd + ld_f64(src->dtype, ps); break;
+      default: return 3;
+    }
+  }
+  return 0;
+}
+
 /* ---- 2-D histogram ----------------------------------------------------------------
  * Binning rule of nca_hist2d: ix = floor((x - x_lo) * sx) in float32 with
  * sx = (float)(nbx / (x_hi - x_lo)); dropped unless 0 <= ix < nbx (NaN dropped).

@@ -226,4 +226,55 @@ int ref_reduce_axes(void* data, int dtype, int ndim, const int64_t* shape, const
   }
 }
 
+// dest (1-D view, dtype dest_dtype) += src scattered by indices through the
+// reference's host::scatter_add_recursive (src/lib/ncarray/host/elementwise.hh:
+// 482-505): for every element i of src in index order, when 0 <= idx[i] <
+// dest.size(), dest[idx[i]] += cast<DestT>(src[i]). indices and src are views
+// of equal shape (ndim, shape, byte strides).
+int ref_scatter_add(void* dest, int dest_dtype, int64_t dest_n, int64_t dest_stride,
+                    const void* idx, int idx_dtype, const void* src, int src_dtype, int ndim,
+                    const int64_t* shape, const int64_t* idx_strides, const int64_t* src_strides) {
+  try {
+    NCArrayView d = make_view(dest, dest_dtype, 1, &dest_n, &dest_stride);
+    NCArrayView ix = make_view(const_cast<void*>(idx), idx_dtype, ndim, shape, idx_strides);
+    NCArrayView sv = make_view(const_cast<void*>(src), src_dtype, ndim, shape, src_strides);
+    auto with_src = [&]<typename DestT, typename IndexT>() {
+      switch ((DType)src_dtype) {
+        case DType::bool_: host::scatter_add_recursive<DestT, IndexT, bool>(d, ix, sv); break;
+        case DType::uint8: host::scatter_add_recursive<DestT, IndexT, std::uint8_t>(d, ix, sv); break;
+        case DType::int16: host::scatter_add_recursive<DestT, IndexT, std::int16_t>(d, ix, sv); break;
+        case DType::int32: host::scatter_add_recursive<DestT, IndexT, std::int32_t>(d, ix, sv); break;
+        case DType::uint32: host::scatter_add_recursive<DestT, IndexT, std::uint32_t>(d, ix, sv); break;
+        case DType::int64: host::scatter_add_recursive<DestT, IndexT, std::int64_t>(d, ix, sv); break;
+        case DType::uint64: host::scatter_add_recursive<DestT, IndexT, std::uint64_t>(d, ix, sv); break;
+        case DType::float32: host::scatter_add_recursive<DestT, IndexT, float>(d, ix, sv); break;
+        case DType::float64: host::scatter_add_recursive<DestT, IndexT, double>(d, ix, sv); break;
+        default: throw std::runtime_error("src dtype not supported by ref_scatter_add");
+      }
+    };
+    auto with_idx = [&]<typename DestT>() {
+      switch ((DType)idx_dtype) {
+        case DType::int32: with_src.template operator()<DestT, std::int32_t>(); break;
+        case DType::int64: with_src.template operator()<DestT, std::int64_t>(); break;
+        case DType::uint32: with_src.template operator()<DestT, std::uint32_t>(); break;
+        case DType::uint64: with_src.template operator()<DestT, std::uint64_t>(); break;
+        default: throw std::runtime_error("index dtype not supported by ref_scatter_add");
+      }
+    };
+    switch ((DType)dest_dtype) {
+      case DType::int32: with_idx.operator()<std::int32_t>(); break;
+      case DType::uint32: with_idx.operator()<std::uint32_t>(); break;
+      case DType::int64: with_idx.operator()<std::int64_t>(); break;
+      case DType::uint64: with_idx.operator()<std::uint64_t>(); break;
+      case DType::float32: with_idx.operator()<float>(); break;
+      case DType::float64: with_idx.operator()<double>(); break;
+      default: throw std::runtime_error("dest dtype not supported by ref_scatter_add");
+    }
+    return 0;
+  } catch (const std::exception& ex) {
+    g_err = ex.what();
+    return 1;
+  }
+}
+
 }  // extern "C"

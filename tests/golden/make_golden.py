@@ -63,6 +63,127 @@ def res_dtype(op, w):
     return w
 
 
+def stencil_weights(kind, rng):
+    w = np.zeros((3, 3, 3))
+    if kind == "7":
+        w[1, 1, 1] = -6.0
+        for dz, dy, dx in ((0, 1, 1), (2, 1, 1), (1, 0, 1), (1, 2, 1), (1, 1, 0), (1, 1, 2)):
+            w[dz, dy, dx] = 1.0
+    elif kind == "27":
+        for dz in range(3):
+            for dy in range(3):
+                for dx in range(3):
+                    far = (dz != 1) + (dy != 1) + (dx != 1)
+                    w[dz, dy, dx] = {0: -128.0, 1: 14.0, 2: 3.0, 3: 1.0}[far] / 30.0
+    else:   # no symmetry, a few zero weights
+        w = rng.normal(size=(3, 3, 3)) * (rng.random((3, 3, 3)) < 0.8)
+    return w.reshape(27)
+
+
+def ref_stencil_step(u, w27, dt):
+    """One step u + dt * sum_o w[o] u[. + o] with zero halo, evaluated by the
+    reference's stack VM over 27 shifted views of a zero-padded copy (the
+    shifted-view pattern of examples/benchmark_binning.cc:36-110). The terms
+    are added in (dz, dy, dx) order, zero weights left out."""
+    nz, ny, nx = u.shape
+    pad = np.zeros((nz + 2, ny + 2, nx + 2))
+    pad[1:-1, 1:-1, 1:-1] = u
+    views, scalars = [], [(F64, slot(dt, F64))]
+    centre = len(views)
+    views.append((pad[1:1 + nz, 1:1 + ny, 1:1 + nx], F64))
+    instrs = [I(2, centre), I(4, 0)]
+    first = True
+    for o in range(27):
+        if w27[o] == 0.0:
+            continue
+        dz, dy, dx = o // 9, (o // 3) % 3, o % 3
+        views.append((pad[dz:dz + nz, dy:dy + ny, dx:dx + nx], F64))
+        scalars.append((F64, slot(w27[o], F64)))
+        instrs += [I(4, len(scalars) - 1), I(2, len(views) - 1), I(16)]
+        if not first:
+            instrs.append(I(14))
+        first = False
+    instrs += [I(16), I(14)]
+    return oracle.ref_expr_eval(instrs, scalars, F64, F64, views, u.shape)
+
+
+def hist_bins(x, y, nbx, nby, xr, yr):
+    """Bin index of every point (-1 = dropped) by the float32 rule of
+    nca_hist2d: floor((x - lo) * s) with s = float32(nb / (hi - lo))."""
+    sx, sy = np.float32(nbx / (xr[1] - xr[0])), np.float32(nby / (yr[1] - yr[0]))
+    fx = np.floor((x - np.float32(xr[0])) * sx)
+    fy = np.floor((y - np.float32(yr[0])) * sy)
+    ok = (fx >= 0) & (fx < nbx) & (fy >= 0) & (fy < nby)
+    return np.where(ok, np.where(ok, fy, 0).astype(np.int64) * nbx + np.where(ok, fx, 0).astype(np.int64), -1)
+
+
+def add_path_cases(store, meta):
+    """Stencil, histogram, batched-reduction and scatter-add cases from the
+    reference's own code (its VM, host::scatter_add_recursive and ArrayImpl
+    reductions), with their own seed so that the cases above stay as they were."""
+    rng = np.random.default_rng(20261204)
+    for kind, shape, iters in (("7", (5, 6, 7), 2), ("27", (4, 9, 8), 3), ("rand", (6, 5, 4), 1)):
+        u0 = rng.normal(size=shape)
+        w = stencil_weights(kind, rng)
+        u = u0
+        for _ in range(iters):
+            u = ref_stencil_step(u, w, 0.1)
+        i = len(meta)
+        store[f"s{i}_in"], store[f"s{i}_w"], store[f"s{i}_out"] = u0, w, u
+        meta.append({"kind": "stencil", "name": kind, "dt": 0.1, "iters": iters})
+    for n, nbx, nby, xr, yr in ((6000, 16, 12, (0.0, 1.0), (0.0, 1.0)), (4000, 7, 9, (-0.5, 1.5), (0.25, 0.75))):
+        centres = rng.uniform(0, 1, (8, 2))
+        sigma = rng.uniform(0.01, 0.1, 8)
+        comp = rng.choice(8, size=n, p=rng.dirichlet(np.full(8, 0.5)))
+        pts = (centres[comp] + rng.normal(size=(n, 2)) * sigma[comp, None]).astype(np.float32)
+        x, y = np.ascontiguousarray(pts[:, 0]), np.ascontiguousarray(pts[:, 1])
+        x[:5] = np.array([np.nan, -0.0, 1.0, np.inf, -1e-8], dtype=np.float32)
+        w = rng.lognormal(0, 1, n).astype(np.float32)
+        b = hist_bins(x, y, nbx, nby, xr, yr)
+        counts = np.zeros(nbx * nby, dtype=np.uint64)
+        wsum = np.zeros(nbx * nby, dtype=np.float64)
+        oracle.ref_scatter_add(counts, U64, b, I64, np.ones(n, dtype=np.uint64), U64)
+        oracle.ref_scatter_add(wsum, F64, b, I64, w, F32)
+        i = len(meta)
+        store[f"h{i}_x"], store[f"h{i}_y"], store[f"h{i}_w"] = x, y, w
+        store[f"h{i}_counts"], store[f"h{i}_wsum"] = counts, wsum
+        meta.append({"kind": "hist", "nbx": nbx, "nby": nby, "xr": list(xr), "yr": list(yr)})
+    # batched reductions: per array the reference's ArrayImpl::sum / mean / max
+    # and the sum of its VM's x*x - x (bfloat16 arrays widened exactly to float32:
+    # the reference has no bfloat16)
+    lens = np.round(np.exp(rng.uniform(np.log(64), np.log(5000), 12))).astype(np.int64)
+    for j, L in enumerate(lens):
+        xf = (np.exp(rng.normal(size=L) * 2.0) * rng.choice([-1.0, 1.0], L)).astype(np.float32)
+        dt = F32
+        if j % 2:
+            raw = (xf.view(np.uint32) >> 16).astype(np.uint16)
+            xf = (raw.astype(np.uint32) << 16).view(np.float32)
+            dt = 22
+        res = {}
+        for name, op in (("sum", 0), ("mean", 1), ("max", 2)):
+            val, odt = oracle.ref_reduce_full(xf, F32, op)
+            res[name] = [float(val), odt]
+        sq = oracle.ref_expr_eval([I(2, 0), I(2, 0), I(16), I(2, 0), I(15)], [], F32, F32, [(xf, F32)], xf.shape)
+        val, odt = oracle.ref_reduce_full(sq, F32, 0)
+        res["sum_sq_m"] = [float(val), odt]
+        i = len(meta)
+        store[f"b{i}_x"] = raw if dt == 22 else xf
+        meta.append({"kind": "batch", "dtype": dt, "ref": res})
+    # scatter-add: dest dtype x index dtype x src dtype, ragged 2-D index/src views
+    for ddt, idt, sdt in ((I64, I64, I32), (U64, I32, U64), (F32, I64, F32), (F64, I32, F32), (I32, U32, I32),
+                          (F64, I64, F64)):
+        shape = (int(rng.integers(3, 9)), int(rng.integers(5, 40)))
+        n_dest = int(rng.integers(5, 200))
+        idx = rng.integers(-5, n_dest + 5, shape).astype(NP[idt] if idt != U32 else np.uint32)
+        src = (rng.normal(size=shape) * 50).astype(NP[sdt]) if sdt in (F32, F64) else \
+            rng.integers(-1000, 1000, shape).astype(NP[sdt])
+        dest = np.zeros(n_dest, dtype=NP[ddt])
+        oracle.ref_scatter_add(dest, ddt, idx, idt, src, sdt)
+        i = len(meta)
+        store[f"x{i}_idx"], store[f"x{i}_src"], store[f"x{i}_dest"] = idx, src, dest
+        meta.append({"kind": "scatter", "dest": ddt, "idx": idt, "src": sdt})
+
+
 def main():
     if oracle.ref() is None:
         oracle.build(with_ref=True)
@@ -135,6 +256,7 @@ def main():
                 store[f"r{i}_ax_{key}"] = y
                 axes[key] = odt
         meta.append({"kind": "reduce", "dtype": dt, "full": {str(k): v for k, v in full.items()}, "axes": axes})
+    add_path_cases(store, meta)
     store["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
     np.savez_compressed(OUT, **store)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(meta)} cases)")

@@ -95,6 +95,50 @@ def test_c4_full_size_counts_oracle(cuda, orc):
     assert int(got.sum()) == inside
 
 
+def test_c4_full_size_weighted_oracle(cuda, orc):
+    """2^27 mixture points with lognormal(0, 1) weights: counts bit-exact and
+    per-bin float32 weight sums within one float32 rounding of the float64
+    oracle (|got - ref| <= 2^-23 |ref|)."""
+    from ncarray_gb300.hist import hist2d
+    rng = np.random.default_rng(SEED + 206)
+    n = 1 << 27
+    centres = rng.uniform(0, 1, (8, 2))
+    sigma = rng.uniform(0.01, 0.1, 8)
+    comp = rng.choice(8, size=n, p=rng.dirichlet(np.full(8, 0.5)))
+    pts = (centres[comp] + rng.normal(size=(n, 2)) * sigma[comp, None]).astype(np.float32)
+    x, y = np.ascontiguousarray(pts[:, 0]), np.ascontiguousarray(pts[:, 1])
+    del pts, comp
+    w = rng.lognormal(0, 1, n).astype(np.float32)
+    counts, wsum = hist2d(nca.NCDevArray.from_host(x), nca.NCDevArray.from_host(y), 1024, 1024,
+                          w=nca.NCDevArray.from_host(w))
+    rc, rw = orc.hist2d(x, y, w, 1024, 1024, 0.0, 1.0, 0.0, 1.0)
+    assert np.array_equal(counts.to_host().reshape(-1), rc)
+    got = wsum.to_host().reshape(-1).astype(np.float64)
+    assert np.all(np.abs(got - rw) <= 2.0**-23 * np.abs(rw) + 1e-30)
+
+
+@pytest.mark.parametrize("kind", ["7", "27"])
+def test_c3_full_size_f32_vs_f64_oracle(cuda, orc, kind):
+    """512^3 float32 grid, 10 Jacobi steps u <- u + 0.1 L(u) with zero halo,
+    against the float64 oracle from the same (float32) start: relative L2
+    error <= 1e-6 and max |err| <= 1e-5 max|u64|."""
+    import torch
+    from ncarray_gb300.stencil import Stencil3D, laplacian7, laplacian27
+    w = (laplacian7() if kind == "7" else laplacian27()).reshape(27)
+    rng = np.random.default_rng(SEED + 207)
+    u0 = rng.standard_normal((512, 512, 512), dtype=np.float32)
+    a = nca.NCDevArray.from_host(u0)
+    b = nca.NCDevArray((512, 512, 512), DType.float32)
+    res = Stencil3D(w, 0.1).iterate(a, b, 10)
+    got = res.to_host().astype(np.float64)
+    torch.cuda.synchronize()
+    want = orc.stencil3d_f64(u0, w, 0.1, 10)
+    err = got - want
+    rel_l2 = float(np.sqrt((err * err).sum() / (want * want).sum()))
+    assert rel_l2 <= 1e-6, rel_l2
+    assert float(np.abs(err).max()) <= 1e-5 * float(np.abs(want).max())
+
+
 def test_c5_full_size_sampled(cuda, orc):
     """20,000 uneven arrays (log-uniform lengths in [64, 2^22], float32 and
     bfloat16 alternately): 300 sampled arrays against the oracle, and

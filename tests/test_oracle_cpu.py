@@ -159,3 +159,72 @@ def test_oracle_bitwise_ops_match_numpy(orc):
         assert np.array_equal(got, want), op
     got = orc.expr_eval([L(0), 13 << 24], [], 8, [(a, 8)], a.shape, 8)
     assert np.array_equal(got, ~a)
+
+
+def test_golden_stencil(orc):
+    """orc_stencil3d_f64 against the reference's VM over 27 shifted views of a
+    zero-padded grid (7-point, 27-point and an asymmetric weight set, 1-3
+    Jacobi steps): bit-exact."""
+    z, meta = golden()
+    n = 0
+    for i, m in enumerate(meta):
+        if m["kind"] != "stencil":
+            continue
+        got = orc.stencil3d_f64(z[f"s{i}_in"], z[f"s{i}_w"], m["dt"], m["iters"])
+        assert got.tobytes() == z[f"s{i}_out"].tobytes(), m["name"]
+        n += 1
+    assert n == 3
+
+
+def test_golden_hist(orc):
+    """orc_hist2d against host::scatter_add_recursive of the reference fed the
+    float32 bin indices (counts uint64, weights summed in float64 in point
+    order): bit-exact, including NaN, inf, -0.0 and out-of-range points."""
+    z, meta = golden()
+    n = 0
+    for i, m in enumerate(meta):
+        if m["kind"] != "hist":
+            continue
+        counts, wsum = orc.hist2d(z[f"h{i}_x"], z[f"h{i}_y"], z[f"h{i}_w"], m["nbx"], m["nby"], *m["xr"], *m["yr"])
+        assert np.array_equal(counts, z[f"h{i}_counts"])
+        assert wsum.tobytes() == z[f"h{i}_wsum"].tobytes()
+        n += 1
+    assert n == 2
+
+
+def test_golden_batch(orc):
+    """orc_batch_reduce (float64, compensated) against the reference's
+    ArrayImpl::sum/mean/max and the sum of its VM's x*x - x, per array: max
+    bit-exact; sums and means within the reference's own float32 error
+    (it accumulates float32 in float32, and rounds x*x - x to float32)."""
+    z, meta = golden()
+    cases = [(i, m) for i, m in enumerate(meta) if m["kind"] == "batch"]
+    assert len(cases) == 12
+    got = orc.batch_reduce([z[f"b{i}_x"] for i, _ in cases], [m["dtype"] for _, m in cases])
+    for (i, m), g in zip(cases, got):
+        raw = z[f"b{i}_x"]
+        x = ((raw.astype(np.uint32) << 16).view(np.float32) if m["dtype"] == 22 else raw).astype(np.float64)
+        n = x.size
+        ref = {k: v[0] for k, v in m["ref"].items()}
+        assert g[2] == ref["max"]
+        b1 = (n + 1) * 2.0**-24 * np.abs(x).sum()
+        assert abs(g[0] - ref["sum"]) <= b1
+        assert abs(g[1] - ref["mean"]) <= b1 / n
+        b2 = (n + 3) * 2.0**-24 * (x * x + np.abs(x)).sum()
+        assert abs(g[3] - ref["sum_sq_m"]) <= b2
+
+
+def test_golden_scatter(orc):
+    """orc_scatter_add against host::scatter_add_recursive (dest dtype x index
+    dtype x source dtype, negative and too-large indices dropped): bit-exact."""
+    z, meta = golden()
+    n = 0
+    for i, m in enumerate(meta):
+        if m["kind"] != "scatter":
+            continue
+        want = z[f"x{i}_dest"]
+        dest = np.zeros_like(want)
+        orc.scatter_add(dest, m["dest"], z[f"x{i}_idx"], m["idx"], z[f"x{i}_src"], m["src"])
+        assert dest.tobytes() == want.tobytes(), m
+        n += 1
+    assert n == 6
