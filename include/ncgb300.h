@@ -216,6 +216,20 @@ int32_t nca_stencil3d(const nca_view* src, const nca_view* dst, const double* we
 int32_t nca_stencil3d_iterate(const nca_view* a, const nca_view* b, const double* weights27,
                               double dt, int32_t iters, void* stream);
 
+/* General stencil of shifted views: for every coordinate c of dest,
+ *   dest[c] = tape(src[c*step + o_0], ..., src[c*step + o_{n-1}]),
+ *   step[d] = src->shape[d] / dest->shape[d] (integer division, >= 1),
+ * where o_i = offsets[i*ndim .. i*ndim+ndim-1] and tape operand i (LOAD_NCARR i)
+ * reads offset i. src and dest have the same ndim; src may have a pointer axis
+ * (NC or SO), dest may not. Every read must lie inside src (checked:
+ * NCA_ERR_SHAPE). At most NCA_MAX_OPERANDS offsets. Does not synchronise, so
+ * it can be captured in a CUDA graph. Replaces Stencil<NDIM>::create/apply
+ * (expression/stencil.hh:76-243) and its kernel generator
+ * (jit/device/rtcompiler.hh:187-385); pro/epilogue code strings
+ * (jit/device/extensions.hh:68-72) have no counterpart. */
+int32_t nca_stencil(const nca_view* src, const nca_view* dest, const int64_t* offsets, int32_t n_offsets,
+                    const nca_tape* tape, void* stream);
+
 /* ---- 2-D histogram ---------------------------------------------------------- */
 /* For each point i with x_i, y_i finite: ix = floor((x_i - x_lo) * sx),
  * iy = floor((y_i - y_lo) * sy) evaluated in float32 with sx = (float)(nbx/(x_hi-x_lo)),
@@ -229,6 +243,18 @@ int32_t nca_stencil3d_iterate(const nca_view* a, const nca_view* b, const double
 int32_t nca_hist2d(const float* x, const float* y, const float* w, int64_t n,
                    int32_t nbx, int32_t nby, double x_lo, double x_hi, double y_lo,
                    double y_hi, uint64_t* counts, float* wsum, void* stream);
+
+/* ---- scatter-add ----------------------------------------------------------- */
+/* For every element i of src, in any order: t = indices[i]; when
+ * 0 <= t < dest->shape[0], dest[t] += (dest dtype) src[i]. dest is a 1-D view
+ * (any byte stride) of int32, uint32, int64, uint64, float32 or float64;
+ * indices (int32, uint32, int64 or uint64) and src (any device dtype) are N-d
+ * views of one shape. Integer sums wrap; float sums round in the order the
+ * additions land (not fixed). No pointer axes. The reference's scatter
+ * primitive: host::scatter_add_recursive (host/elementwise.hh:482-505) and
+ * scatter_add_kernel (device/kernels.cuh:660-680); its Python binding
+ * (pyncarray/binding_builder.hh:708-775) is commented out. */
+int32_t nca_scatter_add(const nca_view* dest, const nca_view* indices, const nca_view* src, void* stream);
 
 /* ---- batched uneven reductions -------------------------------------------- */
 /* One array of a batch: data pointer, length, dtype (float32/bfloat16/float16). */

@@ -84,6 +84,8 @@ EXPORTS = {
     "nca_stencil3d_iterate": (c_int32, [POINTER(View), POINTER(View), POINTER(c_double), c_double, c_int32, c_void_p]),
     "nca_hist2d": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_int32, c_int32, c_double, c_double,
                              c_double, c_double, c_void_p, c_void_p, c_void_p]),
+    "nca_stencil": (c_int32, [POINTER(View), POINTER(View), POINTER(c_int64), c_int32, POINTER(Tape), c_void_p]),
+    "nca_scatter_add": (c_int32, [POINTER(View), POINTER(View), POINTER(View), c_void_p]),
     "nca_batch_create": (c_int32, [POINTER(BatchItem), c_int32, POINTER(c_void_p), c_void_p]),
     "nca_batch_reduce": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "nca_batch_reduce_graph": (c_int32, [c_void_p, c_void_p, c_void_p]),

@@ -365,6 +365,19 @@ class NCDevArray:
             _lib.call("nca_fill", ctypes.byref(self.view_struct()), int(dt), ctypes.byref(slot), current_stream())
         return self
 
+    def scatter_add(self, indices, src) -> "NCDevArray":
+        """self[indices[i]] += src[i] for every element i (indices outside
+        [0, len(self)) are dropped); self is 1-D, indices and src have one
+        shape. Host (numpy) indices or sources are copied to the device first,
+        as the reference binding does (pyncarray/binding_builder.hh:708-775)."""
+        if isinstance(indices, np.ndarray):
+            indices = NCDevArray.from_host(indices)
+        if isinstance(src, np.ndarray):
+            src = NCDevArray.from_host(src)
+        _lib.call("nca_scatter_add", ctypes.byref(self.view_struct()), ctypes.byref(indices.view_struct()),
+                  ctypes.byref(src.view_struct()), current_stream())
+        return self
+
     # ---- expressions ----
     def _expr(self) -> "DevExpr":
         return DevExpr.leaf(self)

@@ -133,6 +133,8 @@ def test_noalloc_special_values(cuda, dt):
                     # must be a positive number or +inf, never NaN
                     assert got > 0 and not np.isnan(got), (name, op_name, got)
                 elif op in (0, 1) and np.isfinite(want) and np.isfinite(got):
-                    assert abs(got - want) <= 2.0**-23 * abs(want), (name, op_name, got, want)
+                    # tied_extremes cancels +-max: only the sum|x|-scaled bound holds
+                    scale = float(np.abs(h.astype(np.float64)).sum()) / (n if op == 1 else 1)
+                    assert abs(got - want) <= 2.0**-23 * abs(want) + 1e-12 * scale, (name, op_name, got, want)
                 else:
                     assert _same(got, want), (name, op_name, got, want)
