@@ -112,10 +112,14 @@ def c2_host(scale_l0: int = 8):
 
 
 def c2_bytes(n: int) -> dict:
-    """Algorithmic bytes of one step over n = elements of the view."""
+    """Algorithmic bytes over n = elements of the view: per kernel, and for
+    the whole step the bytes it must move once -- read x and k, write y and z
+    (4 bytes each), read v, write the axis-2 max (4 B) and argmax (8 B) per
+    kept position. k feeds both expressions but counts once."""
     fused = 12 * n + (4 + 8) * (n // 256) + 1024
     intexpr = 8 * n
-    return {"fused": fused, "int": intexpr, "step": fused + intexpr}
+    step = 16 * n + (4 + 8) * (n // 256) + 1024
+    return {"fused": fused, "int": intexpr, "step": step}
 
 
 class C2Step:
@@ -232,11 +236,32 @@ def timed_flushed(torch, fn, reps, flush_buf):
     return total / reps
 
 
-def op_entry(bytes_, ms, peak, **extra):
+def op_entry(bytes_, ms, peak, elements=None, **extra):
     gbs = bytes_ / (ms * 1e-3) / 1e9
     d = {"GB/s": round(gbs, 1), "frac_of_measured": round(gbs / peak, 4), "ms": round(ms, 4)}
+    if elements:
+        d["Gelements/s"] = round(elements / (ms * 1e-3) / 1e9, 3)
     d.update(extra)
     return d
+
+
+def cpu_entry(fn, bytes_, elements, sample, threads, reps=3):
+    """The oracle port timed on the host cores: best of `reps` wall-clock runs
+    of fn() over a bounded sample of the workload (`bytes_` algorithmic bytes,
+    `elements` units of work in that sample). A reported baseline, not a target."""
+    best = float("inf")
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        best = min(best, time.perf_counter() - t0)
+    return {"GB/s": round(bytes_ / best / 1e9, 3), "Gelements/s": round(elements / best / 1e9, 4),
+            "s": round(best, 4), "cores": threads, "kind": "port", "sample": sample}
+
+
+def _orc_tape(e):
+    """(instrs, scalars, compute dtype) of a DevExpr for the oracle."""
+    from ncarray_gb300.dtype import compute_dtype
+    return list(e.instrs), [(int(d), v) for d, v in e.scalars], int(compute_dtype(e.expr_dtype, e.work))
 
 
 def measure_c1(torch, nca, peak, flush_buf, reps=20):
@@ -267,7 +292,20 @@ def measure_c1(torch, nca, peak, flush_buf, reps=20):
     ref = a * b + np.sqrt(np.abs(c)) - np.float32(0.5) * a
     exact = bool(np.array_equal(out.to_host(), ref))
     rel = abs(float(res["s"].to_host()) - float(np.sum(ref))) / abs(float(np.sum(ref)))
-    return op_entry(32 * n + 2 * 8 * 128 * 128, ms, peak, bound_note="float64 ALU (GB300 FP64 rate) rather than HBM",
+    import oracle
+    ins, sc, cdt = _orc_tape(e)
+    ops = [(a, 11), (b, 11), (c, 11)]
+
+    def cpu_step():
+        y = oracle.expr_eval(ins, sc, cdt, ops, a.shape, 11)
+        oracle.reduce(y, 11, 0, [0])
+        oracle.reduce(y, 11, 2, [0])
+        oracle.reduce(y, 11, 0)
+        oracle.reduce(y, 11, 2)
+
+    cpu = cpu_entry(cpu_step, 32 * n + 2 * 8 * 128 * 128, n, "the whole step (128^3)", omp_threads())
+    return op_entry(32 * n + 2 * 8 * 128 * 128, ms, peak, elements=n, cpu_baseline=cpu,
+                    bound_note="float64 ALU (GB300 FP64 rate) rather than HBM",
                     eager_ms=round(ms_eager, 4), launch="CUDA-graph replay of the step's three evaluate calls",
                     out_bit_exact=exact, sum_rel_err_vs_f64=rel, max_exact=bool(float(res["m"].to_host()) == ref.max()),
                     l2="flushed before every rep (512 MiB write, then 256 MiB read: no dirty lines left)")
@@ -306,8 +344,13 @@ def measure_c3(torch, nca, peak, iters=10):
         t64 = r64._buf.view(torch.float64)
         rel_l2 = float(torch.linalg.vector_norm(t32 - t64) / torch.linalg.vector_norm(t64))
         max_rel = float((t32 - t64).abs().max() / t64.abs().max())
-        out[name] = op_entry(8 * n, ms, peak, per="iteration", rel_l2_err_vs_f64=rel_l2, max_err_rel_to_max=max_rel,
-                             status=status)
+        import oracle
+        sample = src32[:64].cpu().numpy()
+        cpu = cpu_entry(lambda: oracle.stencil3d_f64(sample, w.reshape(27), 0.1, 1), 8 * sample.size, sample.size,
+                        "one float64 iteration on 64 of the 512 z-planes (bytes counted as float32 in/out)",
+                        omp_threads(), reps=2)
+        out[name] = op_entry(8 * n, ms, peak, elements=n, per="iteration", rel_l2_err_vs_f64=rel_l2,
+                             max_err_rel_to_max=max_rel, status=status, cpu_baseline=cpu)
         del a, b, a64, b64, t32, t64
     return out
 
@@ -370,7 +413,15 @@ def measure_c4(torch, nca, peak, reps=5):
             tot += e0.elapsed_time(e1)
         ms = tot / reps
         byts = (12 * P + 16 * 1024 * 1024) if weighted else (8 * P + 8 * 1024 * 1024)
-        out["weighted" if weighted else "counts"] = op_entry(byts, ms, peak, points=P)
+        import oracle
+        ns = 1 << 23
+        xs = x._buf[: 4 * ns].cpu().numpy().view(np.float32)
+        ys = y._buf[: 4 * ns].cpu().numpy().view(np.float32)
+        ws = w._buf[: 4 * ns].cpu().numpy().view(np.float32) if weighted else None
+        cpu = cpu_entry(lambda: oracle.hist2d(xs, ys, ws, 1024, 1024, 0.0, 1.0, 0.0, 1.0),
+                        (12 if weighted else 8) * ns + (16 if weighted else 8) * 1024 * 1024, ns,
+                        "the first 2^23 of the 2^27 points, one thread", 1, reps=2)
+        out["weighted" if weighted else "counts"] = op_entry(byts, ms, peak, elements=P, points=P, cpu_baseline=cpu)
     total = int(counts._buf.view(torch.int64).sum().item())
     out["counts_total"] = total
     return out
@@ -437,6 +488,13 @@ def measure_binning(torch, nca, peak, flush_buf, reps=20):
     b = out.to_host().copy()
     six.evaluate(reductions=[(nca.RedOp.SUM, (1, 3, 5))], red_out=[out])
     c = out.to_host() * np.float32(0.125)
+    import oracle
+    img = data.to_host()
+    ins, sc, cdt = _orc_tape(e_c)
+    views = [(img[i::2, j::2, k::2], 10) for i in range(2) for j in range(2) for k in range(2)]
+    res["cpu_baseline"] = cpu_entry(lambda: oracle.expr_eval(ins, sc, cdt, views, (16, 256, 512), 10), bytes_per,
+                                    16 * 256 * 512, "the whole binning (fused sum of 8 strided views)", omp_threads())
+    res["Gelements/s_fused_views_graph"] = round(16 * 256 * 512 / (res["fused_views_graph"]["us"] * 1e-6) / 1e9, 3)
     res["panels_bit_exact_vs_contiguous"] = bool(np.array_equal(a, b))
     res["reshape_sum_max_rel_diff"] = float(np.max(np.abs(c - a) / np.maximum(np.abs(a), 1e-30)))
     res["l2"] = "flushed before every call (512 MiB write, then 256 MiB read: no dirty lines left)"
@@ -479,7 +537,15 @@ def measure_reductions(torch, nca, peak, reps=50):
         else:
             ok = bool(np.array_equal(got, xh.argmax(axis=axes)))
         res[name] = {"GB/s": round(nbytes / ms / 1e6, 1), "frac_of_measured": round(nbytes / ms / 1e6 / peak, 4),
-                     "us": round(ms * 1e3, 2), "matches_numpy": ok}
+                     "us": round(ms * 1e3, 2), "Gelements/s": round(x.numel() / ms / 1e6, 3), "matches_numpy": ok}
+        if name in ("global_sum", "sum_axis0_4096x16384", "argmax_last_axis_4096x16384"):
+            import oracle
+            part = xh.reshape(-1)[: 1 << 24].reshape((-1,) + tuple(shape[1:])) if len(shape) > 1 else \
+                xh.reshape(-1)[: 1 << 24]
+            ax = None if axes is None else [axes]
+            res[name]["cpu_baseline"] = cpu_entry(lambda: oracle.reduce(part, 10, int(op), ax), part.nbytes,
+                                                  part.size, "the first 2^24 elements, one thread (the "
+                                                  "reference's host reductions are single-threaded)", 1, reps=2)
         del x, d, e, g, outs
         torch.cuda.empty_cache()
     res["l2"] = "inputs 256 MB > L2; no flush"
@@ -555,11 +621,33 @@ def measure_c5(torch, nca, peak, n_arrays=20000):
         raw = a._buf[a._offset: a._offset + a.nbytes].cpu().numpy()
         host.append(raw.view(np.float32) if a.dtype == nca.DType.float32 else raw.view(np.uint16))
         dts.append(10 if a.dtype == nca.DType.float32 else 22)
+    t0 = time.perf_counter()
     ref = oracle.batch_reduce(host, dts, nthreads=omp_threads())
+    cpu_s = time.perf_counter() - t0
+    sbytes = sum(h.nbytes for h in host)
+    selems = sum(h.size for h in host)
+    cpu = {"GB/s": round(sbytes / cpu_s / 1e9, 3), "Gelements/s": round(selems / cpu_s / 1e9, 4), "s": round(cpu_s, 4),
+           "cores": omp_threads(), "kind": "port", "sample": f"{len(pick)} of the {n_arrays} arrays, four results each"}
     g_ = got[pick]
     p_ = plain[pick]
     rel = lambda a_, b_: float(np.max(np.abs(a_ - b_) / np.maximum(np.abs(b_), 1e-300)))  # noqa: E731
-    return op_entry(nbytes, ms_b, peak, arrays=n_arrays, bytes=nbytes, plain_ms=round(ms_p, 3),
+    # the general form (any tapes and reductions per array) on the same four outputs
+    from ncarray_gb300.batch import BatchExpr
+    outs = [(None, nca.RedOp.SUM), (None, nca.RedOp.MEAN), (None, nca.RedOp.MAX), (lambda x: x * x - x, nca.RedOp.SUM)]
+    G = BatchExpr([(a, outs) for a in arrays])
+    G.launch(graph=True)
+    torch.cuda.synchronize()
+    ms_g = timeit(lambda: G.launch(graph=True), 5)
+    gv, _ = G.run(graph=True)
+    general = op_entry(nbytes, ms_g, peak, elements=int(lens.sum()), info=G.info(),
+                       max_rel_err={"sum": rel(gv[pick, 0], ref[:, 0]), "mean": rel(gv[pick, 1], ref[:, 1]),
+                                    "sum_x_times_x_minus_x": rel(gv[pick, 3], ref[:, 3]),
+                                    "max_exact": bool(np.array_equal(gv[pick, 2], ref[:, 2]))},
+                       note="x*x - x rounded as the tape says (two float32 roundings), then summed")
+    del G
+    return op_entry(nbytes, ms_b, peak, elements=int(lens.sum()), arrays=n_arrays, bytes=nbytes, cpu_baseline=cpu,
+                    general_form=general,
+                    plain_ms=round(ms_p, 3),
                     speedup_vs_plain=round(ms_p / ms_b, 2), schedule=sched,
                     batched_max_rel_err={"sum": rel(g_[:, 0], ref[:, 0]), "mean": rel(g_[:, 1], ref[:, 1]),
                                          "sum_x2_minus_x": rel(g_[:, 3], ref[:, 3]),

@@ -140,6 +140,13 @@ int64_t nca_launch_count(void);
  * The reference has no device-side failure reporting (it exits or throws on
  * launch errors only: rtcompiler.hh:68-88, gpuengine.hh:156-158). */
 int32_t nca_device_status(int32_t* status, void* stream);
+/* Diagnostic: one thread waits on an mbarrier that nothing completes, through
+ * the bounded-wait helper of every pipeline kernel, for limit_s seconds
+ * (0.001 .. 2); the wait gives up, records NCA_ERR_TIMEOUT in the status word
+ * nca_device_status reads, and the kernel returns. Shows that a stuck wait ends
+ * with a status and leaves the context usable. No reference counterpart (the
+ * reference has no device-side failure reporting). */
+int32_t nca_wait_probe(double limit_s, void* stream);
 /* Number of JIT kernels compiled / loaded from the disk cache / found in memory. */
 int32_t nca_jit_stats(int64_t* compiled, int64_t* disk_hits, int64_t* mem_hits);
 /* Directory of the on-disk cubin cache (NULL resets to the default). Replaces
@@ -149,6 +156,23 @@ int32_t nca_jit_set_cache_dir(const char* dir);
  * NVRTC for `arch` (e.g. "sm_103a") without touching a device. No reference
  * counterpart (the reference only compiles on first use, rtcompiler.cc:445-510). */
 int32_t nca_jit_selftest(const char* arch, int32_t* n_compiled);
+
+/* ---- launch-schedule autotuner ------------------------------------------- */
+/* Schedules (stencil tile shape and z-march depth; threads per block, vector
+ * groups per thread and grid cap of the elementwise kernels; thread-team size
+ * of row reductions) come from a cache keyed by (op class, dtypes, shape
+ * class), stored as `tune.txt` lines "<key> <values...>" in the JIT cache
+ * directory. mode 0: built-in heuristics only; 1: cached choices where present
+ * (default; NCA_TUNE overrides); 2: a call whose key has no entry first times
+ * every candidate on its stream (it synchronises the stream; skipped while the
+ * stream is being captured and when an output overlaps an operand) and stores
+ * the fastest. The reference launches with a fixed 256-thread block
+ * (engines/gpuengine.hh:93-95) and has no tuner. */
+int32_t nca_tune_set_mode(int32_t mode);
+/* Values cached for `key` (up to cap of them; *n = how many there are, 0 if none). */
+int32_t nca_tune_get(const char* key, int32_t* values, int32_t cap, int32_t* n);
+/* Forgets every cached choice (memory and file). */
+int32_t nca_tune_clear(void);
 
 /* ---- elementwise --------------------------------------------------------- */
 /* out[...] = tape(operands...) over the broadcast of the operands to out's shape.
@@ -299,6 +323,53 @@ int32_t nca_batch_schedule(const nca_batch* batch, int64_t* chunk, int32_t* thre
 /* Status word of the last launch (0 = ok, nonzero = a bounded wait gave up). */
 int32_t nca_batch_status(nca_batch* batch, int32_t* status, void* stream);
 void nca_batch_destroy(nca_batch* batch);
+
+/* ---- general batched reductions ------------------------------------------- */
+/* Items of a general batch: a 1-D array (float32, float64, bfloat16, float16,
+ * int32 or int64) and up to NCA_BATCH_MAX_OUTS outputs, each a tape (an index
+ * into the tapes given to nca_batch_expr_create; a tape over one operand,
+ * LOAD_NCARR 0, with a float32 or float64 result) reduced by an nca_reduce_op.
+ * No reference counterpart: ncarray has no batched API
+ * (pyncarray/utilities.hh:271-314) and runs one synchronous GPUEngine launch
+ * per reduction of each array (engines/gpuengine.hh:222-333). */
+#define NCA_BATCH_MAX_OUTS 4
+typedef struct nca_batch_expr_item {
+  const void* data;
+  int64_t length;
+  int32_t dtype;
+  int32_t n_outs;
+  int32_t tape[NCA_BATCH_MAX_OUTS];
+  int32_t op[NCA_BATCH_MAX_OUTS];
+} nca_batch_expr_item;
+
+/* One result: value (sum, mean, max, min; for argmax/argmin the extreme, or
+ * lowest()/max() of the result dtype when no element beats it) and index
+ * (argmax/argmin: first index of the extreme, 0 when none; else 0). Results
+ * are rows of NCA_BATCH_MAX_OUTS per item, in item order. */
+typedef struct nca_batch_value {
+  double value;
+  int64_t index;
+} nca_batch_value;
+
+typedef struct nca_batch_expr nca_batch_expr;
+
+/* Groups the items by (dtype, outputs), splits the arrays into chunks, uploads
+ * the tables on `stream` and compiles one persistent kernel for the batch
+ * (NVRTC; cached like every JIT kernel). Synchronises `stream`. */
+int32_t nca_batch_expr_create(const nca_batch_expr_item* items, int32_t n_items, const nca_tape* tapes,
+                              int32_t n_tapes, nca_batch_expr** out, void* stream);
+/* One persistent launch for the whole batch; results: device memory, n_items
+ * rows of NCA_BATCH_MAX_OUTS. */
+int32_t nca_batch_expr_run(nca_batch_expr* batch, nca_batch_value* results, void* stream);
+/* The same replayed from a CUDA graph captured on first use (per results
+ * pointer and stream). */
+int32_t nca_batch_expr_run_graph(nca_batch_expr* batch, nca_batch_value* results, void* stream);
+/* The plain form: per item and output one reduction launch of the tape in
+ * float64 (float64 accumulation). */
+int32_t nca_batch_expr_run_plain(nca_batch_expr* batch, nca_batch_value* results, void* stream);
+/* Chunks, distinct programs and CTAs of the persistent launch. */
+int32_t nca_batch_expr_info(const nca_batch_expr* batch, int64_t* n_chunks, int32_t* n_programs, int32_t* ctas);
+void nca_batch_expr_destroy(nca_batch_expr* batch);
 
 #ifdef __cplusplus
 }

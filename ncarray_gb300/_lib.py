@@ -61,6 +61,18 @@ class BatchItem(ctypes.Structure):
     _fields_ = [("data", c_void_p), ("length", c_int64), ("dtype", c_int32), ("reserved", c_int32)]
 
 
+BATCH_MAX_OUTS = 4
+
+
+class BatchExprItem(ctypes.Structure):
+    _fields_ = [("data", c_void_p), ("length", c_int64), ("dtype", c_int32), ("n_outs", c_int32),
+                ("tape", c_int32 * BATCH_MAX_OUTS), ("op", c_int32 * BATCH_MAX_OUTS)]
+
+
+class BatchValue(ctypes.Structure):
+    _fields_ = [("value", c_double), ("index", c_int64)]
+
+
 class BatchResult(ctypes.Structure):
     _fields_ = [("sum", c_double), ("mean", c_double), ("max", c_double), ("sum_sq_m", c_double)]
 
@@ -70,6 +82,10 @@ EXPORTS = {
     "nca_version": (c_int32, []),
     "nca_launch_count": (c_int64, []),
     "nca_device_status": (c_int32, [POINTER(c_int32), c_void_p]),
+    "nca_wait_probe": (c_int32, [c_double, c_void_p]),
+    "nca_tune_set_mode": (c_int32, [c_int32]),
+    "nca_tune_get": (c_int32, [c_char_p, POINTER(c_int32), c_int32, POINTER(c_int32)]),
+    "nca_tune_clear": (c_int32, []),
     "nca_jit_stats": (c_int32, [POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]),
     "nca_jit_set_cache_dir": (c_int32, [c_char_p]),
     "nca_jit_selftest": (c_int32, [c_char_p, POINTER(c_int32)]),
@@ -94,6 +110,12 @@ EXPORTS = {
     "nca_batch_schedule": (c_int32, [c_void_p, POINTER(c_int64), POINTER(c_int32), POINTER(c_int32), POINTER(c_int32)]),
     "nca_batch_status": (c_int32, [c_void_p, POINTER(c_int32), c_void_p]),
     "nca_batch_destroy": (None, [c_void_p]),
+    "nca_batch_expr_create": (c_int32, [POINTER(BatchExprItem), c_int32, POINTER(Tape), c_int32, POINTER(c_void_p), c_void_p]),
+    "nca_batch_expr_run": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "nca_batch_expr_run_graph": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "nca_batch_expr_run_plain": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "nca_batch_expr_info": (c_int32, [c_void_p, POINTER(c_int64), POINTER(c_int32), POINTER(c_int32)]),
+    "nca_batch_expr_destroy": (None, [c_void_p]),
 }
 
 _lib = None

@@ -10,6 +10,7 @@
 // strides, mergeable dims fused), with 128-bit vector access where the layout
 // allows and reductions fused into the same HBM pass.
 #include "jit.hpp"
+#include "tune.hpp"
 
 #include <nvrtc.h>
 #include <sys/stat.h>
@@ -349,6 +350,8 @@ struct Spec {
   int nob = 2;     // kind 7: output tiles (TMA-store double buffering when 2)
   uint32_t pmask = 0, umask = 0, uumask = 0;
   uint32_t ptrmask = 0;   // operands on a pointer axis (kinds 2, 3, 4)
+  int lastcta = 0;   // kind 3, block teams: the last CTA of each kept position merges its partials
+  int block = 256;   // kinds 1, 2: threads per block (NCA_LB)
 };
 
 struct WordLayout {
@@ -461,7 +464,10 @@ static std::string vec_type(int bytes) {
   switch (bytes) { case 16: return "uint4"; case 8: return "uint2"; case 4: return "u32"; case 2: return "unsigned short"; default: return "unsigned char"; }
 }
 
-static std::string gen_eval(const Tape& t) {
+// The tape as statements over the compute type nca_w ending in `return`;
+// operand k is loaded as load_prefix + k + load_suffix.
+static std::string gen_eval(const Tape& t, const std::string& load_prefix = "v[",
+                            const std::string& load_suffix = "][q]") {
   std::ostringstream os;
   std::vector<std::string> st;
   int tmp = 0;
@@ -475,7 +481,7 @@ static std::string gen_eval(const Tape& t) {
     };
     switch (op) {
       case NCA_OP_NOOP: break;
-      case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR: st.push_back("v[" + std::to_string(idx) + "][q]"); break;
+      case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR: st.push_back(load_prefix + std::to_string(idx) + load_suffix); break;
       case NCA_OP_LOAD_CONST: st.push_back("nca_word<nca_w>(s[" + std::to_string(idx) + "])"); break;
       case NCA_OP_IDX: push_tmp("(nca_w)lin"); break;
       default: {
@@ -509,6 +515,18 @@ static std::string gen_eval(const Tape& t) {
   return os.str() + "  return " + res + ";\n";
 }
 
+const char* jit_ctype(int dtype) { return dtinfo(arith_dtype(dtype)).ctype; }
+
+uint64_t jit_scalar_word(int compute_dtype, int scalar_dtype, uint64_t slot) {
+  return scalar_word(compute_dtype, scalar_dtype, slot);
+}
+
+std::string jit_gen_eval(const Tape& t, const std::string& load_prefix, const std::string& load_suffix) {
+  return gen_eval(t, load_prefix, load_suffix);
+}
+
+const char* jit_prelude() { return kPrelude; }
+
 static std::string lim_expr(int dt, bool lowest) {
   switch (arith_dtype(dt)) {
     case NCA_BOOL: return lowest ? "false" : "true";
@@ -536,7 +554,7 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_RED_OPS " << sp.red_ops << "u\n#define NCA_TEAM " << sp.team
      << "\n#define NCA_HAS_OUT " << (sp.has_out ? 1 : 0) << "\n#define NCA_NWORDS " << L.nwords
      << "\n#define NCA_HAS_SUM " << (sp.has_sum ? 1 : 0) << "\n#define NCA_HAS_MAX " << (sp.has_max ? 1 : 0)
-     << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n";
+     << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n#define NCA_LASTCTA " << sp.lastcta << "\n";
   int sum_mode = 1;
   if (sp.nred > 0) {
     const int ra = arith_dtype(sp.r);
@@ -556,6 +574,7 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
   os << "#define NCA_UNROLL " << sp.unroll << "\n#define NCA_KNAME " << kernel_name(sp.kind) << "\n";
   // the staged class asks for sp.minb resident CTAs per SM (register cap)
   if (sp.kind == 6 && sp.minb > 1) os << "#define NCA_LB 256, " << sp.minb << "\n";
+  else if (sp.kind == 1 || sp.kind == 2) os << "#define NCA_LB " << sp.block << "\n";
   else os << "#define NCA_LB 256\n";
   // kind 7: CTAs per SM its shared memory allows (the register cap follows)
   if (sp.kind == 7) os << "#define NCA_K7_MINB " << std::max(1, sp.minb) << "\n#define NCA_NOB " << sp.nob << "\n";
@@ -844,7 +863,12 @@ static std::string arch_for(int dev) {
   return a;
 }
 
-static std::vector<char> nvrtc_compile(const std::string& src, const std::string& arch) {
+static std::vector<char> nvrtc_compile(const std::string& src_in, const std::string& arch) {
+  // NCA_JIT_EXTRA_SOURCE=<text> is appended to every generated source (a
+  // diagnostic hook: extra definitions, or an #error to exercise the compile
+  // failure path)
+  std::string src = src_in;
+  if (const char* extra = getenv("NCA_JIT_EXTRA_SOURCE")) src += std::string("\n") + extra + "\n";
   // NCA_JIT_DUMP=<dir> writes every generated source there (offline inspection)
   if (const char* dump = getenv("NCA_JIT_DUMP")) {
     if (*dump) {
@@ -877,6 +901,8 @@ static std::vector<char> nvrtc_compile(const std::string& src, const std::string
   nvrtcDestroyProgram(&prog);
   return cubin;
 }
+
+void jit_compile_only(const std::string& source, const std::string& arch) { (void)nvrtc_compile(source, arch); }
 
 static std::string nvrtc_version_tag() {
   int a = 0, b = 0;
@@ -937,7 +963,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
   add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
-  add(sp.nob);
+  add(sp.nob); add(sp.lastcta); add(sp.block);
   for (int d : sp.op_dtypes) add(d);
   k += '|';
   for (int m : sp.op_modes) add(m);
@@ -1108,15 +1134,46 @@ static void fill_common_words(const Space& s, const Spec& sp, const Tape& t, con
 }
 
 static void launch(CUfunction fn, int64_t grid, std::vector<uint64_t>& words, cudaStream_t stream,
-                   unsigned smem = 0) {
+                   unsigned smem = 0, unsigned block = 256) {
   if (grid <= 0) return;
   count_launch();
   if (grid > 0x7fffffffLL) fail(NCA_ERR_LIMIT, "grid too large");
   if (smem > 48 * 1024)
     check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem), "smem attribute");
   void* params[] = {words.data()};
-  check_cu(drv().cuLaunchKernel(fn, (unsigned)grid, 1, 1, 256, 1, 1, smem, (CUstream)stream, params, nullptr),
+  check_cu(drv().cuLaunchKernel(fn, (unsigned)grid, 1, 1, block, 1, 1, smem, (CUstream)stream, params, nullptr),
            "cuLaunchKernel");
+}
+
+// byte range [lo, hi) a view can touch (false for pointer-axis views: unknown)
+static bool view_range(const nca_view& v, uintptr_t& lo, uintptr_t& hi) {
+  if (v.pointer_axis >= 0) return false;
+  int64_t a = 0, b = 0;
+  for (int d = 0; d < v.ndim; ++d) {
+    a += v.offsets[d];
+    b += v.offsets[d];
+    if (v.shape[d] == 0) { lo = hi = (uintptr_t)v.data; return true; }
+    const int64_t e = (v.shape[d] - 1) * v.strides[d];
+    if (e < 0) a += e; else b += e;
+  }
+  lo = (uintptr_t)v.data + a;
+  hi = (uintptr_t)v.data + b + dtinfo(v.dtype).size;
+  return true;
+}
+
+// true when running the launch again cannot change what it reads (the
+// outputs overlap no operand): the autotuner may time it several times
+static bool rerun_safe(const nca_view* ops, int nops, const nca_view* outs, int nouts) {
+  for (int j = 0; j < nouts; ++j) {
+    uintptr_t ol, oh;
+    if (!view_range(outs[j], ol, oh)) return false;
+    for (int k = 0; k < nops; ++k) {
+      uintptr_t l, h;
+      if (!view_range(ops[k], l, h)) return false;
+      if (l < oh && ol < h) return false;
+    }
+  }
+  return true;
 }
 
 static int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
@@ -1527,12 +1584,49 @@ void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& 
     if (d == s.nd - 1) dv /= sp.vec;
     compute_magic(dv, w[L.magic + d]);
   }
-  CUfunction fn = kernel_for(sp, tape);
   const int dev = current_device();
   const int64_t groups = total / sp.vec;
-  int64_t grid = std::min<int64_t>(cdiv(std::max<int64_t>(groups, 1), 256 * (int64_t)sp.unroll),
-                                   (int64_t)sm_count(dev) * 8);
-  launch(fn, grid, w, stream);
+  // schedule: threads per block, vector groups per thread per trip (kind 1)
+  // and resident threads per SM the grid is capped at; the autotuner's
+  // cached choice for this (kind, dtypes, operand count, vector width, size
+  // class), else the heuristic (candidate 0)
+  std::vector<std::vector<int>> cands = {{256, sp.unroll, 2048}};
+  if (sp.kind == 1) {
+    for (std::vector<int> c : std::vector<std::vector<int>>{{256, 1, 2048}, {256, 2, 2048}, {256, 4, 2048},
+                                                             {512, 2, 2048}, {128, 4, 1024}, {256, 4, 4096}})
+      if (c != cands[0]) cands.push_back(c);
+  } else {
+    cands.push_back({512, 1, 2048});
+    cands.push_back({128, 1, 2048});
+    cands.push_back({256, 1, 1024});
+    cands.push_back({256, 1, 4096});
+  }
+  std::string key = "ew|k" + std::to_string(sp.kind) + "|" + std::to_string(out.dtype) + "|" +
+                    std::to_string(tape.compute_dtype) + "|";
+  for (int k = 0; k < nops; ++k) key += std::to_string(ops[k].dtype) + ".";
+  key += "|v" + std::to_string(sp.vec) + "|n" + size_class(total) + "|d" + std::to_string(s.nd);
+  auto run = [&](const std::vector<int>& c) {
+    Spec sc = sp;
+    sc.block = c[0];
+    sc.unroll = sp.kind == 1 ? c[1] : 1;
+    CUfunction fn = kernel_for(sc, tape);
+    const int64_t grid = std::min<int64_t>(cdiv(std::max<int64_t>(groups, 1), (int64_t)sc.block * sc.unroll),
+                                           (int64_t)sm_count(dev) * std::max(1, c[2] / sc.block));
+    launch(fn, grid, w, stream, 0, (unsigned)sc.block);
+  };
+  std::vector<int> choice;
+  if (tune_get(key, choice) && choice.size() == 3 && (choice[0] == 128 || choice[0] == 256 || choice[0] == 512) &&
+      choice[1] >= 1 && choice[1] <= 4 && choice[2] >= 256) {
+    run(choice);
+    return;
+  }
+  if (tune_should_search(stream) && groups >= (1 << 16) && rerun_safe(ops, nops, &out, 1)) {
+    const int best = tune_pick(stream, (int)cands.size(), [&](int i) { run(cands[(size_t)i]); });
+    tune_put(key, cands[(size_t)best]);
+    run(cands[(size_t)best]);
+    return;
+  }
+  run(cands[0]);
 }
 
 int reduce_out_dtype(int op, int in_dt) {
@@ -1632,47 +1726,90 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     // (whole sectors per load, where one thread per row uses half of each, and
     // no warp-wide tree) and one thread up to 8; over several reduced dims, one
     // thread below 64 elements (its offsets from a per-block table)
-    if (s.nd - sp.nkept == 1) sp.team = RN >= 4096 ? 256 : (RN >= 1024 ? 32 : (RN > 8 ? 2 : 1));
-    else sp.team = RN >= 4096 ? 256 : (RN >= 64 ? 32 : 1);
-    const int64_t tpb = 256 / sp.team;
-    const int64_t target = (int64_t)sms * tpb * 8;
-    int64_t S = 1;
-    if (KN < target && RN > 0) {
-      S = cdiv(target, KN);
-      S = std::min<int64_t>(S, std::max<int64_t>(1, RN / ((int64_t)sp.team * sp.vec * 8)));
+    const int heur_team = s.nd - sp.nkept == 1 ? (RN >= 4096 ? 256 : (RN >= 1024 ? 32 : (RN > 8 ? 2 : 1)))
+                                               : (RN >= 4096 ? 256 : (RN >= 64 ? 32 : 1));
+    // one launch (plus its finalize) with teams of `team` threads
+    auto run_team = [&](int team) {
+      sp.team = team;
+      sp.lastcta = 0;
+      const int64_t tpb = 256 / sp.team;
+      const int64_t target = (int64_t)sms * tpb * 8;
+      int64_t S = 1;
+      if (KN < target && RN > 0) {
+        S = cdiv(target, KN);
+        S = std::min<int64_t>(S, std::max<int64_t>(1, RN / ((int64_t)sp.team * sp.vec * 8)));
+      }
+      int64_t C = RN > 0 ? cdiv(RN, S) : 0;
+      C = cdiv(C, sp.vec) * sp.vec;
+      if (C > 0) S = cdiv(RN, C);
+      if (S < 1) S = 1;
+      const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
+      std::vector<uint64_t> w;
+      fill_common_words(s, sp, tape, L, w);
+      w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+      // 32-bit coordinate decoding (magic-number division) when every index fits
+      {
+        bool small = KN * S < (1ll << 31) && RN < (1ll << 31);
+        for (int d = 0; d < s.nd; ++d) if (s.shape[d] >= (1ll << 31)) small = false;
+        if (small) for (int d = 0; d < s.nd; ++d) compute_magic(std::max<int64_t>(s.shape[d], 1), w[L.magic + d]);
+        sp.idx32 = small ? 1 : 0;
+      }
+      // block teams over few kept positions (global reductions): the CTA that
+      // stores the last partial of a kept position merges them in the order the
+      // finalize pass uses (one arrival counter per kept position, zeroed here),
+      // so there is no second launch and the result is the same
+      sp.lastcta = (S > 1 && sp.team == 256 && KN <= 64) ? 1 : 0;
+      const size_t pbytes = S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0;
+      const size_t cbytes = sp.lastcta ? ((size_t)KN * 4 + 255) / 256 * 256 : 0;
+      StreamScratch part(pbytes + cbytes, stream);
+      if (S > 1) {
+        uint64_t* p = (uint64_t*)part.ptr;
+        if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
+        if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+        if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+        if (sp.lastcta) {
+          w[L.aux] = (uint64_t)(uintptr_t)p;
+          check_cuda(cudaMemsetAsync(p, 0, cbytes, stream), "arrival counters");
+        }
+      }
+      CUfunction fn = kernel_for(sp, tape);
+      // warp and smaller teams stride over their units from a few blocks per SM
+      // (one-thread teams build their reduced-offset table once per block); a
+      // block team takes one unit per block, so one block's tree and store
+      // overlap the other blocks' loads
+      const int64_t groups = cdiv(KN * S, tpb);
+      launch(fn, sp.team == 256 ? groups : std::min<int64_t>(groups, (int64_t)sms * 8), w, stream);
+      if (S > 1 && !sp.lastcta) {
+        launch_finalize(sp, tape, KN, sms, w, stream);
+      }
+    };
+    // team size: the autotuner's cached choice for this (dtypes, ops, reduced
+    // and kept size class, dims), else the heuristic; rows of 64 to 64 Ki
+    // elements are searched in search mode
+    std::string key = "red|k3|" + std::to_string(tape.compute_dtype) + "|" + std::to_string(red_ops) + "|";
+    for (int k = 0; k < nops; ++k) key += std::to_string(ops[k].dtype) + ".";
+    key += "|r" + size_class(RN) + "|k" + size_class(KN) + "|d" + std::to_string(s.nd) + "." + std::to_string(sp.nkept) +
+           "|v" + std::to_string(sp.vec);
+    const bool one_dim = s.nd - sp.nkept == 1;
+    auto team_ok = [&](int t) { return t == 2 || t == 32 || t == 256 || (t == 1 && (one_dim || RN < 64)); };
+    std::vector<int> choice;
+    if (tune_get(key, choice) && choice.size() == 1 && team_ok(choice[0])) {
+      run_team(choice[0]);
+      return;
     }
-    int64_t C = RN > 0 ? cdiv(RN, S) : 0;
-    C = cdiv(C, sp.vec) * sp.vec;
-    if (C > 0) S = cdiv(RN, C);
-    if (S < 1) S = 1;
-    const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
-    std::vector<uint64_t> w;
-    fill_common_words(s, sp, tape, L, w);
-    w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
-    // 32-bit coordinate decoding (magic-number division) when every index fits
-    {
-      bool small = KN * S < (1ll << 31) && RN < (1ll << 31);
-      for (int d = 0; d < s.nd; ++d) if (s.shape[d] >= (1ll << 31)) small = false;
-      if (small) for (int d = 0; d < s.nd; ++d) compute_magic(std::max<int64_t>(s.shape[d], 1), w[L.magic + d]);
-      sp.idx32 = small ? 1 : 0;
+    std::vector<nca_view> routs;
+    for (int k = 0; k < nred; ++k) routs.push_back(rv[(size_t)k].out);
+    if (RN >= 64 && RN <= 65536 && KN * RN >= (1 << 16) && tune_should_search(stream) &&
+        rerun_safe(ops, nops, routs.data(), nred)) {
+      std::vector<int> cands = {heur_team};
+      for (int t : {1, 2, 32, 256})
+        if (t != heur_team && team_ok(t) && (t != 1 || RN <= 1024)) cands.push_back(t);
+      const int best = tune_pick(stream, (int)cands.size(), [&](int i) { run_team(cands[(size_t)i]); });
+      tune_put(key, {cands[(size_t)best]});
+      run_team(cands[(size_t)best]);
+      return;
     }
-    StreamScratch part(S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0, stream);
-    if (S > 1) {
-      uint64_t* p = (uint64_t*)part.ptr;
-      if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
-      if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
-      if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
-    }
-    CUfunction fn = kernel_for(sp, tape);
-    // warp and smaller teams stride over their units from a few blocks per SM
-    // (one-thread teams build their reduced-offset table once per block); a
-    // block team takes one unit per block, so one block's tree and store
-    // overlap the other blocks' loads
-    const int64_t groups = cdiv(KN * S, tpb);
-    launch(fn, sp.team == 256 ? groups : std::min<int64_t>(groups, (int64_t)sms * 8), w, stream);
-    if (S > 1) {
-      launch_finalize(sp, tape, KN, sms, w, stream);
-    }
+    run_team(heur_team);
     return;
   }
   // innermost dim kept. Operands strided along it but contiguous along another
@@ -1770,6 +1907,12 @@ int jit_selftest(const char* arch) {
         nvrtc_compile(gen_source(s2, t), a);
         ++n;
       }
+      if (kind == 3) {   // block teams whose last CTA merges the partials
+        Spec s3 = sp;
+        s3.lastcta = 1;
+        nvrtc_compile(gen_source(s3, t), a);
+        ++n;
+      }
     }
     // kinds 2, 3, 4 with operand 0 on a pointer axis (first two dtype rows)
     if (&d - &dts[0] < 2) {
@@ -1845,6 +1988,7 @@ int jit_selftest(const char* arch) {
     nvrtc_compile(gen_source(sp, t), a);
     ++n;
   }
+  n += batch_expr_selftest(a.c_str());
   return n;
 }
 

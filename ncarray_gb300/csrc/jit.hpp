@@ -44,8 +44,21 @@ std::string jit_cache_dir();
 // device. Used by the JIT engine and available to other modules.
 CUfunction jit_get(const std::string& source, const char* name);
 
+// The device prelude of every JIT kernel (types, 16-bit float conversions,
+// the tape operations), and the statements of a tape over the compute type
+// `nca_w` ending in `return` (operand k loaded as prefix + k + suffix).
+const char* jit_prelude();
+std::string jit_gen_eval(const Tape& t, const std::string& load_prefix, const std::string& load_suffix);
+// A tape scalar as the 64-bit argument word of compute dtype `compute_dtype`.
+uint64_t jit_scalar_word(int compute_dtype, int scalar_dtype, uint64_t slot);
+// C type name of an arithmetic dtype in generated device code.
+const char* jit_ctype(int dtype);
+
 }  // namespace nca
 
 namespace nca {
 int jit_selftest(const char* arch);
+// NVRTC compile of `source` for `arch` without loading it (fails on errors)
+void jit_compile_only(const std::string& source, const std::string& arch);
+int batch_expr_selftest(const char* arch);
 }

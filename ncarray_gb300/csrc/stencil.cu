@@ -24,10 +24,13 @@
 
 #include "common.hpp"
 #include "mbar.cuh"
+#include "tune.hpp"
 
 namespace {
 
-constexpr int TX = 64, TY = 16, NST = 4, THREADS = 256;
+// tile shapes (x, y) of the TMA kernel; each has (TX / 4) * TY = THREADS threads
+constexpr int NST = 4, THREADS = 256;
+constexpr int kTiles[3][2] = {{64, 16}, {128, 8}, {32, 32}};
 constexpr unsigned long long kWaitNs = 2000000000ull;
 
 static __device__ int g_stencil_status;
@@ -40,17 +43,17 @@ struct Weights {
 };
 
 template <class T> __host__ __device__ constexpr int halo_x() { return 16 / (int)sizeof(T); }
-template <class T> __host__ __device__ constexpr int box_w() { return TX + 2 * halo_x<T>(); }
-template <class T> __host__ __device__ constexpr int stage_bytes() {
-  return ((box_w<T>() * (TY + 2) * (int)sizeof(T)) + 127) / 128 * 128;
+template <class T, int TX> __host__ __device__ constexpr int box_w() { return TX + 2 * halo_x<T>(); }
+template <class T, int TX, int TY> __host__ __device__ constexpr int stage_bytes() {
+  return ((box_w<T, TX>() * (TY + 2) * (int)sizeof(T)) + 127) / 128 * 128;
 }
 
 
 using nca_dev::mbar_wait;
 
-template <class T>
+template <class T, int TX, int TY>
 __device__ __forceinline__ void issue_plane(const CUtensorMap* tmap, uint32_t dst, uint32_t bar, int x, int y, int z) {
-  constexpr uint32_t bytes = (uint32_t)(box_w<T>() * (TY + 2) * sizeof(T));
+  constexpr uint32_t bytes = (uint32_t)(box_w<T, TX>() * (TY + 2) * sizeof(T));
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
@@ -83,12 +86,13 @@ __device__ __forceinline__ T fmaT(T a, T b, T c) {
 // offset depends only on how many of its components are non-zero: w[13] for
 // none, w[12] for one, w[9] for two, w[0] for three), evaluated per plane from
 // the in-plane centre, face and corner sums (12 instead of 27 FMAs a point).
-template <class T, int MODE>
+template <class T, int MODE, int TX, int TY>
 __global__ void __launch_bounds__(THREADS)
 stencil_tma_kernel(const __grid_constant__ CUtensorMap tmap, T* __restrict__ out, int nx, int ny, int nz,
                    int zt, const __grid_constant__ Weights<T> W) {
   extern __shared__ __align__(128) unsigned char smem[];
-  constexpr int BW = box_w<T>(), HX = halo_x<T>(), SB = stage_bytes<T>();
+  static_assert((TX / 4) * TY == THREADS, "a tile has one thread per 4 outputs");
+  constexpr int BW = box_w<T, TX>(), HX = halo_x<T>(), SB = stage_bytes<T, TX, TY>();
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + NST * SB);
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * zt;
   const int zend = min(z0 + zt, nz);
@@ -105,7 +109,7 @@ stencil_tma_kernel(const __grid_constant__ CUtensorMap tmap, T* __restrict__ out
   int issued = 0;
   if (threadIdx.x == 0) {
     for (; issued < NST && issued < nplanes; ++issued)
-      issue_plane<T>(&tmap, sbase + issued * SB, bbase + 8 * issued, x0 - HX, y0 - 1, z0 - 1 + issued);
+      issue_plane<T, TX, TY>(&tmap, sbase + issued * SB, bbase + 8 * issued, x0 - HX, y0 - 1, z0 - 1 + issued);
   }
   // acc_a: output p-1 (missing only plane p's dz=+1 part), acc_b: output p
   // (has plane p-1's dz=-1 part), cen: centre value of output p-1
@@ -199,7 +203,7 @@ stencil_tma_kernel(const __grid_constant__ CUtensorMap tmap, T* __restrict__ out
     }
     if (__syncthreads_or(ok ? 0 : 1)) { timed_out = true; break; }
     if (threadIdx.x == 0 && issued < nplanes) {
-      issue_plane<T>(&tmap, sbase + st * SB, bbase + 8 * st, x0 - HX, y0 - 1, z0 - 1 + issued);
+      issue_plane<T, TX, TY>(&tmap, sbase + st * SB, bbase + 8 * st, x0 - HX, y0 - 1, z0 - 1 + issued);
       ++issued;
     }
   }
@@ -298,11 +302,11 @@ bool tma_ok(const Grid3& g) {
   return g.nx % 4 == 0 && ((uintptr_t)g.base % 16) == 0 && nca::drv().cuTensorMapEncodeTiled != nullptr;
 }
 
-template <class T>
+template <class T, int TX, int TY>
 void encode_map(CUtensorMap* m, const Grid3& g) {
   const cuuint64_t dims[3] = {(cuuint64_t)g.nx, (cuuint64_t)g.ny, (cuuint64_t)g.nz};
   const cuuint64_t strides[2] = {(cuuint64_t)g.nx * sizeof(T), (cuuint64_t)g.nx * g.ny * sizeof(T)};
-  const cuuint32_t box[3] = {(cuuint32_t)box_w<T>(), (cuuint32_t)(TY + 2), 1u};
+  const cuuint32_t box[3] = {(cuuint32_t)box_w<T, TX>(), (cuuint32_t)(TY + 2), 1u};
   const cuuint32_t estr[3] = {1u, 1u, 1u};
   nca::check_cu(nca::drv().cuTensorMapEncodeTiled(
                     m, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
@@ -311,22 +315,70 @@ void encode_map(CUtensorMap* m, const Grid3& g) {
                 "cuTensorMapEncodeTiled");
 }
 
+template <class T, int TX, int TY>
+void launch_tma(const Grid3& src, const Grid3& dst, const Weights<T>& W, int mode, int zt, cudaStream_t s) {
+  CUtensorMap m;
+  encode_map<T, TX, TY>(&m, src);
+  dim3 grid((src.nx + TX - 1) / TX, (src.ny + TY - 1) / TY, (src.nz + zt - 1) / zt);
+  const size_t smem = NST * stage_bytes<T, TX, TY>() + NST * 8;
+  if (mode == 1)
+    stencil_tma_kernel<T, 1, TX, TY><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
+  else if (mode == 2)
+    stencil_tma_kernel<T, 2, TX, TY><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
+  else
+    stencil_tma_kernel<T, 0, TX, TY><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
+  nca::check_cuda(cudaGetLastError(), "stencil launch");
+  nca::count_launch();
+}
+
+template <class T>
+void launch_tile(int tile, const Grid3& src, const Grid3& dst, const Weights<T>& W, int mode, int zt, cudaStream_t s) {
+  switch (tile) {
+    case 1: launch_tma<T, kTiles[1][0], kTiles[1][1]>(src, dst, W, mode, zt, s); break;
+    case 2: launch_tma<T, kTiles[2][0], kTiles[2][1]>(src, dst, W, mode, zt, s); break;
+    default: launch_tma<T, kTiles[0][0], kTiles[0][1]>(src, dst, W, mode, zt, s); break;
+  }
+}
+
+// Tile shape and z-march depth: the autotuner's cached choice for this
+// (dtype, stencil form, grid size class), else the built-in heuristic; in
+// search mode a miss times every (tile, depth) candidate on this call first.
+template <class T>
+void tma_schedule(const Grid3& src, const Grid3& dst, const Weights<T>& W, int mode, cudaStream_t s, int& tile,
+                  int& zt) {
+  using namespace nca;
+  tile = 0;
+  zt = src.nz >= 256 ? 32 : (src.nz >= 64 ? 16 : 8);
+  const std::string key = std::string("stencil3d|") + (sizeof(T) == 4 ? "f32" : "f64") + "|" + std::to_string(mode) +
+                          "|" + size_class(src.nz) + "x" + size_class(src.ny) + "x" + size_class(src.nx);
+  std::vector<int> v;
+  if (tune_get(key, v) && v.size() == 2 && v[0] >= 0 && v[0] < 3 && v[1] >= 1) {
+    tile = v[0];
+    zt = v[1];
+    return;
+  }
+  if (!tune_should_search(s)) return;
+  std::vector<std::pair<int, int>> cands;
+  for (int t = 0; t < 3; ++t)
+    for (int z : {8, 16, 32, 64})
+      if (z <= std::max(8, src.nz)) cands.push_back({t, z});
+  const int best = tune_pick(s, (int)cands.size(), [&](int i) {
+    launch_tile<T>(cands[(size_t)i].first, src, dst, W, mode, cands[(size_t)i].second, s);
+  });
+  tile = cands[(size_t)best].first;
+  zt = cands[(size_t)best].second;
+  tune_put(key, {tile, zt});
+}
+
 template <class T>
 void launch_one(const Grid3& src, const Grid3& dst, const Weights<T>& W, int mode, cudaStream_t s) {
   using namespace nca;
   const int dev = current_device();
   if (tma_ok(src) && tma_ok(dst)) {
-    CUtensorMap m;
-    encode_map<T>(&m, src);
-    const int zt = src.nz >= 256 ? 32 : (src.nz >= 64 ? 16 : 8);
-    dim3 grid((src.nx + TX - 1) / TX, (src.ny + TY - 1) / TY, (src.nz + zt - 1) / zt);
-    const size_t smem = NST * stage_bytes<T>() + NST * 8;
-    if (mode == 1)
-      stencil_tma_kernel<T, 1><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
-    else if (mode == 2)
-      stencil_tma_kernel<T, 2><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
-    else
-      stencil_tma_kernel<T, 0><<<grid, THREADS, smem, s>>>(m, (T*)dst.mut, src.nx, src.ny, src.nz, zt, W);
+    int tile = 0, zt = 8;
+    tma_schedule<T>(src, dst, W, mode, s, tile, zt);
+    launch_tile<T>(tile, src, dst, W, mode, zt, s);
+    return;
   } else {
     const long long n = (long long)src.nx * src.ny * src.nz;
     const long long blocks = std::min<long long>((n + THREADS - 1) / THREADS, (long long)sm_count(dev) * 32);
@@ -383,6 +435,32 @@ int stencil_read_status(cudaStream_t s) {
   return v;
 }
 }  // namespace nca
+
+namespace {
+// One thread waits, through the bounded-wait helper every pipeline kernel
+// uses, on an mbarrier that expects one arrival which never comes (no copy is
+// issued, so none is in flight); after limit_ns it records NCA_ERR_TIMEOUT in
+// the stencil status word and returns.
+__global__ void wait_probe_kernel(unsigned long long limit_ns) {
+  __shared__ __align__(8) unsigned long long bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  if (!mbar_wait(b, 0u, limit_ns)) atomicExch(&g_stencil_status, (int)NCA_ERR_TIMEOUT);
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(b) : "memory");
+}
+}  // namespace
+
+extern "C" int32_t nca_wait_probe(double limit_s, void* stream) {
+  return nca::guarded([&] {
+    using namespace nca;
+    if (!(limit_s >= 1e-3 && limit_s <= 2.0)) fail(NCA_ERR_INVALID, "limit %g s: 0.001 .. 2 s", limit_s);
+    wait_probe_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((unsigned long long)(limit_s * 1e9));
+    check_cuda(cudaGetLastError(), "wait probe launch");
+    count_launch();
+  });
+}
 
 extern "C" int32_t nca_stencil3d(const nca_view* src, const nca_view* dst, const double* weights27, double dt,
                                  void* stream) {
