@@ -347,12 +347,19 @@ int orc_expr_eval(const uint32_t* instrs, int n_instrs, const int* scalar_dtypes
  * (ndim 0 for a full reduction). Sum output dtype: sum_type of the input
  * (op_traits.hh:72-76,380-410; 16-bit floats -> float32); mean -> float64;
  * max/min -> input dtype (16-bit floats -> float32); arg* -> int64. */
+/* Neumaier-compensated float64 sum. Once the running sum is infinite or NaN
+ * its compensation is meaningless (inf - inf would make it NaN), so it is no
+ * longer updated and neum_get returns the sum alone: an all -inf input sums to
+ * -inf, as the reference's plain accumulation gives. */
 typedef struct { double s, c; } neum;
 static void neum_add(neum* a, double x) {
   const double t = a->s + x;
-  if (fabs(a->s) >= fabs(x)) a->c += (a->s - t) + x; else a->c += (x - t) + a->s;
+  if (isfinite(t)) {
+    if (fabs(a->s) >= fabs(x)) a->c += (a->s - t) + x; else a->c += (x - t) + a->s;
+  }
   a->s = t;
 }
+static double neum_get(const neum* a) { return isfinite(a->s) ? a->s + a->c : a->s; }
 
 static int is_float_dt(int dt) { return dt == D_F32 || dt == D_F64 || dt == D_BF16 || dt == D_F16; }
 static int is_signed_dt(int dt) {
@@ -467,11 +474,11 @@ int orc_reduce(const orc_view* src, int op, uint32_t axes_mask, const orc_view* 
     for (int d = kept - 1; d >= 0; --d) { po += (rem % kshape[d]) * out->strides[d]; rem /= kshape[d]; }
     if (op == 0) {
       const int sdt = sum_dt(dt);
-      if (isf) { const double s = fs[j].s + fs[j].c; st_f64(sdt, po, s); }
+      if (isf) { const double s = neum_get(&fs[j]); st_f64(sdt, po, s); }
       else memcpy(po, &is[j], dsize(sdt));
     } else if (op == 1) {
       double s;
-      if (isf) s = fs[j].s + fs[j].c;
+      if (isf) s = neum_get(&fs[j]);
       else s = is_signed_dt(dt) ? (double)(int64_t)is[j] : (double)is[j];
       *(double*)po = s / (double)RN;
     } else if (op == 2 || op == 3) {
@@ -605,10 +612,10 @@ int orc_batch_reduce(const orc_item* items, int n, orc_result* res, int nthreads
       neum_add(&q, xd * xd - xd);
       if (x > mx) mx = x;
     }
-    res[i].sum = s.s + s.c;
-    res[i].mean = (s.s + s.c) / (double)L;
+    res[i].sum = neum_get(&s);
+    res[i].mean = neum_get(&s) / (double)L;
     res[i].max = (double)mx;
-    res[i].sum_sq_m = q.s + q.c;
+    res[i].sum_sq_m = neum_get(&q);
   }
   return 0;
 }
