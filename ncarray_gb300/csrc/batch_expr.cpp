@@ -221,7 +221,7 @@ template <class F> __device__ __forceinline__ void nca_bwalk_f32(const void* bas
   for (i64 i = threadIdx.x; i < head; i += blockDim.x) f.one(__ldcs(p + i), b + i);
   const i64 nv = (n - head) >> 2;
   const float4* pv = (const float4*)(p + head);
-#pragma unroll 4
+#pragma unroll NCA_BUNROLL
   for (i64 k = threadIdx.x; k < nv; k += blockDim.x) {
     const float4 v = __ldcs(pv + k);
     const i64 i = b + head + 4 * k;
@@ -239,7 +239,7 @@ template <int HALF, class F> __device__ __forceinline__ void nca_bwalk_h16(const
   for (i64 i = threadIdx.x; i < head; i += blockDim.x) f.one(cv(__ldcs(p + i)), b + i);
   const i64 nv = (n - head) >> 3;
   const uint4* pv = (const uint4*)(p + head);
-#pragma unroll 4
+#pragma unroll NCA_BUNROLL
   for (i64 k = threadIdx.x; k < nv; k += blockDim.x) {
     const uint4 v = __ldcs(pv + k);
     const i64 i = b + head + 8 * k;
@@ -258,7 +258,7 @@ template <class F> __device__ __forceinline__ void nca_bwalk_f64(const void* bas
   for (i64 i = threadIdx.x; i < head; i += blockDim.x) f.one(__ldcs(p + i), b + i);
   const i64 nv = (n - head) >> 1;
   const double2* pv = (const double2*)(p + head);
-#pragma unroll 4
+#pragma unroll NCA_BUNROLL
   for (i64 k = threadIdx.x; k < nv; k += blockDim.x) {
     const double2 v = __ldcs(pv + k);
     f.two(v.x, v.y, b + head + 2 * k);
@@ -339,7 +339,9 @@ struct nca_batch_expr {
   void* d_cnt = nullptr;
   void* d_scal = nullptr;
   long long nchunks = 0;
-  long long chunk_bytes = 128 * 1024;
+  long long chunk_bytes = 512 * 1024;   // fastest with 4 loads in flight and 4 CTAs per SM on 20,000 uneven arrays
+  int unroll = 4;          // 16-byte loads per thread issued together in the walkers
+  int ctas_per_sm = 4;
   int ctas = 0;
   cudaGraphExec_t graph = nullptr;
   void* graph_results = nullptr;
@@ -375,7 +377,7 @@ std::vector<Acc> prog_accs(const Program& p, int* acc_of_out) {
 
 std::string gen_batch_source(const nca_batch_expr& b) {
   std::ostringstream os;
-  os << nca::jit_prelude() << kBatchCommon;
+  os << nca::jit_prelude() << "#define NCA_BUNROLL " << b.unroll << "\n" << kBatchCommon;
   for (size_t k = 0; k < b.tapes.size(); ++k) os << tape_fn(b.tapes[k], (int)k);
   for (size_t p = 0; p < b.progs.size(); ++p) {
     const Program& pg = b.progs[p];
@@ -429,8 +431,12 @@ std::string gen_batch_source(const nca_batch_expr& b) {
     for (size_t a = 0; a < accs.size(); ++a) {
       const int K = accs[a].kind;
       const char* IDX = accs[a].idx ? "true" : "false";
+      // identity: lowest() / max() of the result type, the value an output
+      // reports when no element beats it (partials without a candidate are
+      // skipped by the indexed merge)
+      const std::string R = nca::jit_ctype(b.tapes[(size_t)accs[a].tape].result_dtype);
       os << "  {\n    NcaBPart m; m.s = 0.0; m.i = -1; m.pad = 0;\n"
-         << "    m.v = " << (K == 1 ? "-" : "") << "__longlong_as_double(0x7ff0000000000000ll);\n"
+         << "    m.v = (double)" << (K == 1 ? "nca_blo<" : "nca_bhi<") << R << ">();\n"
          << "    for (int k = threadIdx.x; k < it.nchunks; k += blockDim.x) {\n"
          << "      NcaBPart o = A.parts[(long long)(it.first_chunk + k) * " << NCA_BATCH_MAX_OUTS << " + " << a << "];\n"
          << "      nca_bmerge<" << K << ", " << IDX << ">(m, o);\n    }\n"
@@ -512,7 +518,10 @@ extern "C" int32_t nca_batch_expr_create(const nca_batch_expr_item* items, int32
     std::map<Program, int> prog_id;
     std::vector<ItemDev> hi((size_t)n_items);
     std::vector<ChunkDev> hc;
+    // schedule knobs: chunk bytes, 16-byte loads per thread in flight, CTAs per SM
     if (const char* e = getenv("NCA_BATCH_EXPR_CHUNK")) b->chunk_bytes = std::max(4096ll, atoll(e));
+    if (const char* e = getenv("NCA_BATCH_EXPR_UNROLL")) b->unroll = std::max(1, std::min(16, atoi(e)));
+    if (const char* e = getenv("NCA_BATCH_EXPR_CTAS")) b->ctas_per_sm = std::max(1, std::min(8, atoi(e)));
     for (int i = 0; i < n_items; ++i) {
       const nca_batch_expr_item& it = items[i];
       if (it.length < 0) fail(NCA_ERR_SHAPE, "item %d: negative length", i);
@@ -565,7 +574,7 @@ extern "C" int32_t nca_batch_expr_create(const nca_batch_expr_item* items, int32
     b->fn = jit_get(gen_batch_source(*b), "nca_batch_expr");
     int per_sm = 0;
     check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->fn, 256, 0), "occupancy");
-    b->ctas = sm_count(b->dev) * std::max(1, std::min(per_sm, 4));
+    b->ctas = sm_count(b->dev) * std::max(1, std::min(per_sm, b->ctas_per_sm));
     check_cuda(cudaStreamSynchronize(s), "batch table upload");
     *out = b;
   });
@@ -683,6 +692,7 @@ namespace nca {
 // programs over float32, bfloat16, float64 and int32 inputs with every op.
 int batch_expr_selftest(const char* arch) {
   nca_batch_expr b;
+  b.unroll = 4;
   auto mk = [](std::vector<uint32_t> ins, int w) {
     Tape t;
     t.instrs = std::move(ins);

@@ -350,7 +350,7 @@ struct Spec {
   int nob = 2;     // kind 7: output tiles (TMA-store double buffering when 2)
   uint32_t pmask = 0, umask = 0, uumask = 0;
   uint32_t ptrmask = 0;   // operands on a pointer axis (kinds 2, 3, 4)
-  int lastcta = 0;   // kind 3, block teams: the last CTA of each kept position merges its partials
+  int lastcta = 0;   // kinds 3 (block teams) and 4: the last CTA over a set of kept positions merges their partials
   int block = 256;   // kinds 1, 2: threads per block (NCA_LB)
 };
 
@@ -506,7 +506,13 @@ static std::string gen_eval(const Tape& t, const std::string& load_prefix = "v["
             case NCA_OP_BOR: f = "nca_bor"; break; case NCA_OP_XOR: f = "nca_xor"; break;
             default: fail(NCA_ERR_UNSUPPORTED, "opcode %d", op);
           }
-          push_tmp(std::string(f) + "<nca_w>(" + a + ", " + b + ")");
+          // a multiplication by a tape constant (power-of-two constants
+          // scale exactly on the integer pipe for float64)
+          const bool ca = a.rfind("nca_word<", 0) == 0, cb = b.rfind("nca_word<", 0) == 0;
+          if (op == NCA_OP_MUL && (ca != cb))
+            push_tmp("nca_mulc<nca_w>(" + (cb ? a : b) + ", " + (cb ? b : a) + ")");
+          else
+            push_tmp(std::string(f) + "<nca_w>(" + a + ", " + b + ")");
         }
       }
     }
@@ -883,8 +889,8 @@ static std::vector<char> nvrtc_compile(const std::string& src_in, const std::str
   if (nvrtcCreateProgram(&prog, src.c_str(), "nca_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
     fail(NCA_ERR_COMPILE, "nvrtcCreateProgram failed");
   const std::string archopt = "--gpu-architecture=" + arch;
-  const char* opts[] = {archopt.c_str(), "--fmad=false", "--std=c++17", "-DNDEBUG", "-lineinfo"};
-  nvrtcResult r = nvrtcCompileProgram(prog, 5, opts);
+  const char* opts[] = {archopt.c_str(), "--fmad=false", "--std=c++17", "-DNDEBUG", "-lineinfo", "--device-int128"};
+  nvrtcResult r = nvrtcCompileProgram(prog, 6, opts);
   if (r != NVRTC_SUCCESS) {
     size_t n = 0;
     nvrtcGetProgramLogSize(prog, &n);
@@ -1233,11 +1239,14 @@ static int find_staged(const Space& s, uint32_t& tmask, int& nt) {
 // the finalize pass: a block per kept position when there are very few (global
 // reductions), a warp per kept position when there are few, a thread per kept
 // position when there are many
-static void launch_finalize(const Spec& sp, const Tape& tape, int64_t KN, int sms, std::vector<uint64_t>& w,
-                            cudaStream_t stream) {
+static void launch_finalize(const Spec& sp, const Tape& tape, int64_t KN, int64_t S, int sms,
+                            std::vector<uint64_t>& w, cudaStream_t stream) {
   Spec fs = sp;
   fs.kind = 5;
-  fs.team = KN >= 32768 ? 1 : (KN <= 64 ? 256 : 32);
+  // few splits: a thread walks them in order (no shuffle tree, whose adds are
+  // float64 instructions for float64 sums and GB300 runs those slowly)
+  fs.team = (KN >= 32768 || (S <= 32 && KN > 64)) ? 1 : (KN <= 64 ? 256 : 32);
+  fs.lastcta = 0;
   CUfunction ff = kernel_for(fs, tape);
   const int64_t per_block = fs.team == 1 ? 256 : (fs.team == 32 ? 8 : 1);   // kept positions per block
   launch(ff, std::min<int64_t>(cdiv(KN, per_block), (int64_t)sms * 8), w, stream);
@@ -1298,7 +1307,7 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   // block of rb loop indices: a divisor of the fastest loop extent whose
   // (loop index, q) rows fill whole 128-byte boxes, at most 128 of them, the
   // largest whose stages fit in the 227 KiB a CTA may use. 128 rows per block
-  // and 2 stages measured best on the C2 views (about 97 KiB per CTA, two
+  // and 2 stages measured best on the permuted (8,256,256,64) float32 views (about 97 KiB per CTA, two
   // CTAs per SM: 5.6 TB/s against 5.4 TB/s for 64 rows and 3 stages, three
   // CTAs per SM)
   const int64_t budget = 227 * 1024;
@@ -1505,7 +1514,7 @@ static void launch_staged(const Space& s, Spec sp, const Tape& tape, int qd, uin
   }
   launch(fn, units * S, w, stream, smem);
   if (split) {
-    launch_finalize(sp, tape, KN, sms, w, stream);
+    launch_finalize(sp, tape, KN, S, sms, w, stream);
   }
 }
 
@@ -1780,7 +1789,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       const int64_t groups = cdiv(KN * S, tpb);
       launch(fn, sp.team == 256 ? groups : std::min<int64_t>(groups, (int64_t)sms * 8), w, stream);
       if (S > 1 && !sp.lastcta) {
-        launch_finalize(sp, tape, KN, sms, w, stream);
+        launch_finalize(sp, tape, KN, S, sms, w, stream);
       }
     };
     // team size: the autotuner's cached choice for this (dtypes, ops, reduced
@@ -1829,27 +1838,70 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
   plan_vec(s, sp, 4, out != nullptr);
   const int64_t KG = KN / sp.vec;
-  const int64_t target = (int64_t)sms * 1024;
-  int64_t S = 1;
-  if (KG < target) S = std::min<int64_t>(cdiv(target, KG), std::max<int64_t>(1, RN / 8));
-  int64_t C = cdiv(RN, S);
-  S = cdiv(RN, C);
-  const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
-  std::vector<uint64_t> w;
-  fill_common_words(s, sp, tape, L, w);
-  w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
-  StreamScratch part(S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0, stream);
-  if (S > 1) {
-    uint64_t* p = (uint64_t*)part.ptr;
-    if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
-    if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
-    if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+  // one launch (plus its finalize) with `unroll` rows per thread in flight and
+  // splits chosen for `tps` threads per SM
+  auto run_k4 = [&](int unroll, int tps, int lastcta) {
+    sp.unroll = unroll;
+    const int64_t target = (int64_t)sms * tps;
+    int64_t S = 1;
+    if (KG < target) S = std::min<int64_t>(cdiv(target, KG), std::max<int64_t>(1, RN / 8));
+    int64_t C = cdiv(RN, S);
+    S = cdiv(RN, C);
+    const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
+    std::vector<uint64_t> w;
+    fill_common_words(s, sp, tape, L, w);
+    w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+    // lastcta: when the kept groups fill whole 256-thread blocks, the last of
+    // the S blocks over a set of kept groups merges their partials (one arrival
+    // counter per set, zeroed here) instead of a finalize launch; a tuned choice
+    sp.lastcta = (lastcta && S > 1 && KG % 256 == 0) ? 1 : 0;
+    const size_t pbytes = S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0;
+    const size_t cbytes = sp.lastcta ? ((size_t)(KG / 256) * 4 + 255) / 256 * 256 : 0;
+    StreamScratch part(pbytes + cbytes, stream);
+    if (S > 1) {
+      uint64_t* p = (uint64_t*)part.ptr;
+      if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
+      if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+      if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+      if (sp.lastcta) {
+        w[L.aux] = (uint64_t)(uintptr_t)p;
+        check_cuda(cudaMemsetAsync(p, 0, cbytes, stream), "arrival counters");
+      }
+    }
+    CUfunction fn = kernel_for(sp, tape);
+    launch(fn, cdiv(KG * S, 256), w, stream);
+    if (S > 1 && !sp.lastcta) {
+      launch_finalize(sp, tape, KN, S, sms, w, stream);
+    }
+  };
+  // schedule: the autotuner's cached choice for this (dtypes, ops, stored
+  // value, kept and reduced size class, dims), else 4 rows in flight and 1024
+  // threads per SM; searched (rows 4 / 8, 512 / 1024 / 2048 threads per SM)
+  // when the kernel writes nothing it reads
+  std::string key = "red|k4|" + std::to_string(tape.compute_dtype) + "|" + std::to_string(red_ops) + "|o" +
+                    std::to_string(out ? out->dtype : -1) + "|";
+  for (int k = 0; k < nops; ++k) key += std::to_string(ops[k].dtype) + ".";
+  key += "|r" + size_class(RN) + "|k" + size_class(KN) + "|d" + std::to_string(s.nd) + "|v" + std::to_string(sp.vec);
+  std::vector<int> choice;
+  if (tune_get(key, choice) && choice.size() == 3 && (choice[0] == 4 || choice[0] == 8) &&
+      (choice[1] == 512 || choice[1] == 1024 || choice[1] == 2048) && (choice[2] == 0 || choice[2] == 1)) {
+    run_k4(choice[0], choice[1], choice[2]);
+    return;
   }
-  CUfunction fn = kernel_for(sp, tape);
-  launch(fn, cdiv(KG * S, 256), w, stream);
-  if (S > 1) {
-    launch_finalize(sp, tape, KN, sms, w, stream);
+  std::vector<nca_view> routs;
+  for (int k = 0; k < nred; ++k) routs.push_back(rv[(size_t)k].out);
+  if (out) routs.push_back(*out);
+  if (KN * RN >= (1 << 16) && tune_should_search(stream) && rerun_safe(ops, nops, routs.data(), (int)routs.size())) {
+    const std::vector<std::vector<int>> cands = {{4, 1024, 0}, {8, 1024, 0}, {4, 2048, 0}, {8, 2048, 0}, {8, 512, 0},
+                                                 {4, 1024, 1}, {8, 512, 1}};
+    const int best = tune_pick(stream, (int)cands.size(), [&](int i) {
+      run_k4(cands[(size_t)i][0], cands[(size_t)i][1], cands[(size_t)i][2]);
+    });
+    tune_put(key, cands[(size_t)best]);
+    run_k4(cands[(size_t)best][0], cands[(size_t)best][1], cands[(size_t)best][2]);
+    return;
   }
+  run_k4(4, 1024, 0);
 }
 
 }  // namespace nca
@@ -1861,7 +1913,7 @@ namespace nca {
 int jit_selftest(const char* arch) {
   const std::string a = arch ? arch : "sm_103a";
   int n = 0;
-  // tape: a*b + sqrt(abs(c)) - 0.5*a  (C1 shape of ops)
+  // tape: a*b + sqrt(abs(c)) - 0.5*a
   Tape t;
   auto I = [](int op, int idx) { return (uint32_t)(op << 24) | (uint32_t)idx; };
   t.instrs = {I(NCA_OP_LOAD_NCARR, 0), I(NCA_OP_LOAD_NCARR, 1), I(NCA_OP_MUL, 0),
@@ -1907,7 +1959,7 @@ int jit_selftest(const char* arch) {
         nvrtc_compile(gen_source(s2, t), a);
         ++n;
       }
-      if (kind == 3) {   // block teams whose last CTA merges the partials
+      if (kind == 3 || kind == 4) {   // last CTA over a set of kept positions merges the partials
         Spec s3 = sp;
         s3.lastcta = 1;
         nvrtc_compile(gen_source(s3, t), a);
