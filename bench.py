@@ -355,11 +355,10 @@ def measure_c3(torch, nca, peak, iters=10):
     return out
 
 
-def c4_points(torch, nca):
-    """2^27 (x, y) float32 points from a mixture of 8 Gaussians (centres
+def c4_points(torch, nca, P=1 << 27):
+    """P = 2^27 (x, y) float32 points from a mixture of 8 Gaussians (centres
     uniform in [0,1)^2, sigma 0.01-0.1, Dirichlet(0.5) weights) and lognormal
     weights, generated on the device from a seed."""
-    P = 1 << 27
     rng = np.random.default_rng(SEED + 3)
     centres = rng.uniform(0, 1, (8, 2))
     sigma = rng.uniform(0.01, 0.1, 8)
@@ -677,12 +676,16 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
             e = da * db + nca.sqrt(abs(dc)) - 0.5 * da
         out = nca.NCDevArray(e.shape, e.dtype)
         fn = lambda: e.evaluate(out=out, reductions=[(nca.RedOp.SUM, 0), (nca.RedOp.MAX, 0)])  # noqa: E731
-    elif op == "c4":
+    elif op in ("c4", "c4-counts", "c4-small", "c4-counts-small"):
+        # the small forms: 2^25 points (128 MB per array, above L2) for full captures
         from ncarray_gb300.hist import hist2d_into
-        x, y, w = c4_points(torch, nca)
+        x, y, w = c4_points(torch, nca, (1 << 25) if op.endswith("small") else (1 << 27))
         counts = nca.NCDevArray((1024, 1024), nca.DType.uint64).fill(0)
         wsum = nca.NCDevArray((1024, 1024), nca.DType.float32).fill(0.0)
-        fn = lambda: hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0), w, wsum)  # noqa: E731
+        if not op.startswith("c4-counts"):
+            fn = lambda: hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0), w, wsum)  # noqa: E731
+        else:
+            fn = lambda: hist2d_into(x, y, counts, (0.0, 1.0), (0.0, 1.0))  # noqa: E731
     elif op == "binning":
         # the fused sum of eight strided views of a (32, 512, 1024) image (2x2x2 bins)
         data = nca.NCDevArray((32, 512, 1024), nca.DType.float32)

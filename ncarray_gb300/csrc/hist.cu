@@ -35,6 +35,8 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
+#include <string>
 
 #include "common.hpp"
 #include "mbar.cuh"
@@ -42,7 +44,8 @@
 namespace {
 
 constexpr int THREADS = 256;
-constexpr int TB = 16384;               // bins per tile (local index fits in uint16)
+constexpr int TB_LOG2 = 14;
+constexpr int TB = 1 << TB_LOG2;        // bins per tile (local index fits in uint16)
 constexpr int MAX_TILES = 256;          // partitioned path limit (4 Mi bins; tile index fits in uint8)
 constexpr int SAMPLE = 32;              // 1 block of 1024 points in SAMPLE is counted in pass 1
 constexpr int CHUNK = 2048;             // points per chunk in the scatter pass
@@ -56,7 +59,6 @@ constexpr int FPAD = 16;                // fill counters 128 bytes apart (uint64
 constexpr int EPAD = 32;                // estimate counters 128 bytes apart (uint32)
 static_assert(MAX_TILES * NSUB <= 4 * SCAN_THREADS, "bucket scan size");
 
-constexpr unsigned OVERFLOW = 0x80000000u;   // staged record that did not fit its bucket
 constexpr unsigned long long kWaitNs = 2000000000ull;   // bound of every mbarrier wait
 
 static __device__ int g_hist_status;   // NCA_ERR_TIMEOUT after a wait that ran out
@@ -71,6 +73,20 @@ __device__ __forceinline__ int bin_of(const Bins& B, float x, float y) {
   const float fy = floorf(__fmul_rn(__fsub_rn(y, B.yl), B.sy));
   if (!(fx >= 0.0f && fx < B.fnx && fy >= 0.0f && fy < B.fny)) return -1;
   return (int)fy * B.nbx + (int)fx;
+}
+
+// The same bin for grids of at most 2^22 bins (the partitioned path), without
+// float-to-int conversions: the floor of v in [0, 2^23) is the low mantissa
+// bits of v + 2^23 rounded toward zero, and v >= 0 / v < n (integer n) accept
+// exactly the values whose floor floorf(v) does.
+constexpr unsigned NO_BIN = 0xffffffffu;
+__device__ __forceinline__ unsigned tile_bin_of(const Bins& B, float x, float y) {
+  const float fx = __fmul_rn(__fsub_rn(x, B.xl), B.sx);
+  const float fy = __fmul_rn(__fsub_rn(y, B.yl), B.sy);
+  if (!(fx >= 0.0f && fx < B.fnx && fy >= 0.0f && fy < B.fny)) return NO_BIN;
+  const unsigned ix = (unsigned)__float_as_int(__fadd_rz(fx, 8388608.0f)) & 0x7fffffu;
+  const unsigned iy = (unsigned)__float_as_int(__fadd_rz(fy, 8388608.0f)) & 0x7fffffu;
+  return iy * (unsigned)B.nbx + ix;
 }
 
 // ---- direct path: global atomics per point -------------------------------------
@@ -199,11 +215,9 @@ tile_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y, co
   __shared__ unsigned cnt[MAX_TILES];
   __shared__ unsigned loff[MAX_TILES];      // start of each tile's run in the staged chunk
   __shared__ unsigned wpre[THREADS / 32];
-  __shared__ unsigned base[MAX_TILES];      // start of this CTA's run in the record arrays
-  __shared__ unsigned avail[MAX_TILES];     // how many of the run fit in the bucket
-  __shared__ unsigned short sbin[CHUNK];    // the chunk's records ordered by tile
+  __shared__ uint2 tinfo[MAX_TILES];        // (record index - staged position, end of the stored part)
+  __shared__ unsigned srec[CHUNK];          // the chunk's bins ordered by tile
   __shared__ float sw[WEIGHTED ? CHUNK : 1];
-  __shared__ unsigned sdst[CHUNK];          // record index, or OVERFLOW | tile
   const long long nfull = n / CHUNK, nchunks = (n + CHUNK - 1) / CHUNK;
   const int sub = (int)(blockIdx.x % NSUB);
   if (threadIdx.x == 0) {
@@ -234,28 +248,30 @@ tile_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y, co
     if (__syncthreads_or(ok ? 0 : 1)) { failed = true; break; }
     const long long c0 = ch * CHUNK;
     const float* bx = buf + (size_t)(b * NA) * CHUNK;
-    int bins[PER_THREAD];
+    unsigned bins[PER_THREAD];
     float ws[PER_THREAD];
 #pragma unroll
     for (int k = 0; k < PER_THREAD; ++k) {
       const int li = threadIdx.x + k * THREADS;
-      bins[k] = -1;
       ws[k] = 0.f;
       if (full) {
-        bins[k] = bin_of(B, bx[li], bx[CHUNK + li]);
+        bins[k] = tile_bin_of(B, bx[li], bx[CHUNK + li]);
         if (WEIGHTED) ws[k] = bx[2 * CHUNK + li];
       } else if (c0 + li < n) {
-        bins[k] = bin_of(B, __ldcs(x + c0 + li), __ldcs(y + c0 + li));
+        bins[k] = tile_bin_of(B, __ldcs(x + c0 + li), __ldcs(y + c0 + li));
         if (WEIGHTED) ws[k] = __ldcs(w + c0 + li);
+      } else {
+        bins[k] = NO_BIN;
       }
     }
     // rank within the CTA's run of the tile (lanes of a warp on the same
     // counter are serialised by the shared-memory unit, one issue slot each)
     unsigned rank[PER_THREAD];
 #pragma unroll
-    for (int k = 0; k < PER_THREAD; ++k) rank[k] = bins[k] >= 0 ? atomicAdd(&cnt[bins[k] / TB], 1u) : 0u;
+    for (int k = 0; k < PER_THREAD; ++k) rank[k] = bins[k] != NO_BIN ? atomicAdd(&cnt[bins[k] >> TB_LOG2], 1u) : 0u;
     __syncthreads();
-    // exclusive scan of the tile counts (ntiles <= MAX_TILES == THREADS)
+    // exclusive scan of the tile counts (ntiles <= MAX_TILES == THREADS); the
+    // thread of tile t then reserves the tile's run in its bucket
     {
       const int t = threadIdx.x, lane = t & 31, wp = t >> 5;
       const unsigned v0 = t < ntiles ? cnt[t] : 0u;
@@ -278,43 +294,41 @@ tile_scatter_kernel(const float* __restrict__ x, const float* __restrict__ y, co
         if (lane < THREADS / 32) wpre[lane] = q - q0;
       }
       __syncthreads();
-      loff[t] = v - v0 + wpre[wp];
-    }
-    for (int t = threadIdx.x; t < ntiles; t += THREADS) {
-      base[t] = 0;
-      avail[t] = 0;
-      if (cnt[t]) {
+      const unsigned lo = v - v0 + wpre[wp];
+      loff[t] = lo;
+      if (v0) {
         // positions [p, p + cnt) are this CTA's; the part below the capacity is
         // always written, so every position below min(fill, cap) holds a record
-        const int v = t * NSUB + sub;
-        const unsigned long long p = atomicAdd(fill + (long long)v * FPAD, (unsigned long long)cnt[t]);
-        const long long room = cap[v] - (long long)p;
-        base[t] = (unsigned)(off[v] + (long long)p);
-        avail[t] = room <= 0 ? 0u : (room >= (long long)cnt[t] ? cnt[t] : (unsigned)room);
+        const int vb = t * NSUB + sub;
+        const unsigned long long p = atomicAdd(fill + (long long)vb * FPAD, (unsigned long long)v0);
+        const long long room = cap[vb] - (long long)p;
+        const unsigned avail = room <= 0 ? 0u : (room >= (long long)v0 ? v0 : (unsigned)room);
+        tinfo[t] = make_uint2((unsigned)(off[vb] + (long long)p) - lo, lo + avail);
       }
     }
     __syncthreads();
-    // stage the records in tile order with their destinations
+    // stage the bins in tile order
 #pragma unroll
     for (int k = 0; k < PER_THREAD; ++k) {
-      const int bn = bins[k];
-      if (bn < 0) continue;
-      const int t = bn / TB;
-      const unsigned j = loff[t] + rank[k];
-      sbin[j] = (unsigned short)(bn - t * TB);
-      sdst[j] = rank[k] < avail[t] ? base[t] + rank[k] : (OVERFLOW | (unsigned)t);
+      if (bins[k] == NO_BIN) continue;
+      const unsigned j = loff[bins[k] >> TB_LOG2] + rank[k];
+      srec[j] = bins[k];
       if (WEIGHTED) sw[j] = ws[k];
     }
     __syncthreads();
-    // consecutive threads write consecutive records of a tile's run
+    // consecutive threads write consecutive records of a tile's run; a record
+    // past its bucket's capacity is added with global atomics instead
     const unsigned total = loff[ntiles - 1] + cnt[ntiles - 1];
-    for (unsigned j = threadIdx.x; j < total; j += THREADS) {
-      const unsigned d = sdst[j];
-      if (!(d & OVERFLOW)) {
-        rec_bin[d] = sbin[j];
-        if (WEIGHTED) rec_w[d] = sw[j];
+#pragma unroll
+    for (int k = 0; k < PER_THREAD; ++k) {
+      const unsigned j = threadIdx.x + k * THREADS;
+      if (j >= total) break;
+      const unsigned bn = srec[j];
+      const uint2 ti = tinfo[bn >> TB_LOG2];
+      if (j < ti.y) {
+        rec_bin[ti.x + j] = (unsigned short)(bn & (TB - 1));
+        if (WEIGHTED) rec_w[ti.x + j] = sw[j];
       } else {
-        const long long bn = (long long)(d & ~OVERFLOW) * TB + sbin[j];
         atomicAdd(counts + bn, 1ull);
         if (WEIGHTED) atomicAdd(wacc + bn, (double)sw[j]);
       }
@@ -537,7 +551,10 @@ extern "C" int32_t nca_hist2d(const float* x, const float* y, const float* w, in
     unsigned long long* cnt = (unsigned long long*)counts;
     // the bulk copies of the partitioned path need 16-byte aligned point arrays
     const bool aligned = ((uintptr_t)x % 16 == 0) && ((uintptr_t)y % 16 == 0) && (!weighted || (uintptr_t)w % 16 == 0);
-    if (ntiles > MAX_TILES || n < (1 << 20) || !aligned) {
+    // NCA_HIST_PATH=direct forces the direct path (tests and measurements)
+    const char* hp = getenv("NCA_HIST_PATH");
+    const std::string path = hp ? hp : "";
+    if (ntiles > MAX_TILES || n < (1 << 20) || !aligned || path == "direct") {
       StreamScratch acc(weighted ? (size_t)nbins * sizeof(double) : 0, s);
       double* wacc = (double*)acc.ptr;
       if (weighted) check_cuda(cudaMemsetAsync(wacc, 0, (size_t)nbins * sizeof(double), s), "memset weights");
