@@ -721,6 +721,50 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
         B = Batch(arrays)
         B.run(graph=False)
         fn = lambda: B.run(graph=False)  # noqa: E731
+    elif op == "c5-general-small":
+        # the general batched form (any tapes and reductions) on 1,000 of the uneven arrays
+        from ncarray_gb300.batch import BatchExpr
+        _, _, arrays, _, _ = c5_arrays(torch, nca, 1000)
+        outs = [(None, nca.RedOp.SUM), (None, nca.RedOp.MEAN), (None, nca.RedOp.MAX),
+                (lambda x: x * x - x, nca.RedOp.SUM)]
+        G = BatchExpr([(a, outs) for a in arrays])
+        G.launch(graph=False)
+        fn = lambda: G.launch(graph=False)  # noqa: E731
+    elif op == "red-axis0":
+        # float32 (4096, 16384) summed over axis 0 (256 MB read, 64 KB written)
+        x = torch.randn(4096 * 16384, device="cuda", dtype=torch.float32)
+        e = nca.NCDevArray((4096, 16384), nca.DType.float32, _buf=x.view(torch.uint8))._expr()
+        fn = lambda: e.evaluate(reductions=[(nca.RedOp.SUM, 0)])  # noqa: E731
+    elif op == "scatter-add":
+        # 2^26 float32 values scattered into 2^20 float32 entries by int64 indices
+        # drawn from 8 narrow Gaussians (768 MB read)
+        g = torch.Generator(device="cuda").manual_seed(SEED + 11)
+        n, nd = 1 << 26, 1 << 20
+        cen = torch.randint(0, nd, (8,), generator=g, device="cuda").float()
+        comp = torch.randint(0, 8, (n,), generator=g, device="cuda")
+        idx = (cen[comp] + torch.randn(n, generator=g, device="cuda") * 2000.0).long().clamp_(0, nd - 1)
+        src = torch.rand(n, generator=g, device="cuda")
+        di = nca.NCDevArray((n,), nca.DType.int64, _buf=idx.view(torch.uint8))
+        ds = nca.NCDevArray((n,), nca.DType.float32, _buf=src.view(torch.uint8))
+        dest = nca.NCDevArray((nd,), nca.DType.float32).fill(0.0)
+        fn = lambda: dest.scatter_add(di, ds)  # noqa: E731
+    elif op == "stencil-binning":
+        # the pixel-binning stencil of the reference's benchmark through the
+        # general stencil: 8 offset views of a (32, 512, 1024) float32 image
+        from ncarray_gb300.stencil import Stencil
+        src = nca.NCDevArray((32, 512, 1024), nca.DType.float32)
+        src._buf.view(torch.float32).copy_(torch.rand(32 * 512 * 1024, device="cuda"))
+        offs = [(p, r, c) for p in range(2) for r in range(2) for c in range(2)]
+
+        def binning(views):
+            e = nca.DevExpr.leaf(views[0])
+            for v in views[1:]:
+                e = e + v
+            return e * np.float32(0.125)
+
+        st = Stencil.create(offs, binning, nca.DType.float32, is_pointer_axis=[0, 0, 0])
+        out = nca.NCDevArray((16, 256, 512), nca.DType.float32)
+        fn = lambda: st.apply(src, out)  # noqa: E731
     else:
         raise SystemExit(f"unknown --profile-op {op}")
     for _ in range(steps):

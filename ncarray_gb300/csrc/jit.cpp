@@ -352,6 +352,8 @@ struct Spec {
   uint32_t ptrmask = 0;   // operands on a pointer axis (kinds 2, 3, 4)
   int lastcta = 0;   // kinds 3 (block teams) and 4: the last CTA over a set of kept positions merges their partials
   int block = 256;   // kinds 1, 2: threads per block (NCA_LB)
+  int k4r = 0;       // kind 4: row lanes per warp (row-lane form, one reduced dim rd); 0: thread per column group
+  int rd = 0;
 };
 
 struct WordLayout {
@@ -553,6 +555,10 @@ static std::string lim_expr(int dt, bool lowest) {
 static std::string gen_source(const Spec& sp, const Tape& t) {
   const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
   std::ostringstream os;
+  // NCA_F64_INTPIPE=0: float64 sqrt, constant products and comparisons as
+  // float64 instructions instead of their integer-pipe forms (measurements)
+  static const bool f64_fp = [] { const char* e = getenv("NCA_F64_INTPIPE"); return e && e[0] == '0'; }();
+  if (f64_fp) os << "#define NCA_F64_FP 1\n";
   os << kPrelude;
   os << "#define NCA_NOPS " << sp.nops << "\n#define NCA_ND " << sp.nd << "\n#define NCA_NRED " << sp.nred
      << "\n#define NCA_KIND " << sp.kind << "\n#define NCA_VEC " << sp.vec << "\n#define NCA_IDX32 " << sp.idx32
@@ -560,7 +566,8 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_RED_OPS " << sp.red_ops << "u\n#define NCA_TEAM " << sp.team
      << "\n#define NCA_HAS_OUT " << (sp.has_out ? 1 : 0) << "\n#define NCA_NWORDS " << L.nwords
      << "\n#define NCA_HAS_SUM " << (sp.has_sum ? 1 : 0) << "\n#define NCA_HAS_MAX " << (sp.has_max ? 1 : 0)
-     << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n#define NCA_LASTCTA " << sp.lastcta << "\n";
+     << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n#define NCA_LASTCTA " << sp.lastcta
+     << "\n#define NCA_K4R " << sp.k4r << "\n#define NCA_RD " << sp.rd << "\n";
   int sum_mode = 1;
   if (sp.nred > 0) {
     const int ra = arith_dtype(sp.r);
@@ -969,7 +976,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
   add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
-  add(sp.nob); add(sp.lastcta); add(sp.block);
+  add(sp.nob); add(sp.lastcta); add(sp.block); add(sp.k4r); add(sp.rd);
   for (int d : sp.op_dtypes) add(d);
   k += '|';
   for (int m : sp.op_modes) add(m);
@@ -1648,6 +1655,19 @@ int reduce_out_dtype(int op, int in_dt) {
   fail(NCA_ERR_INVALID, "unknown reduction op %d", op);
 }
 
+// NCA_K4_ROWS=0 keeps outer reductions on the thread-per-column-group form
+// unless a tuned choice names the row-lane form; NCA_K4_ROWS=2 has the
+// row-lane form merge its splits in a finalize launch instead of the last CTA
+// (tests and measurements)
+static bool k4r_off() {
+  const char* e = getenv("NCA_K4_ROWS");
+  return e && e[0] == '0';
+}
+static int k4r_lastcta() {
+  const char* e = getenv("NCA_K4_ROWS");
+  return (e && e[0] == '2') ? 0 : 1;
+}
+
 void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
                  const nca_reduction* reds, int nred, cudaStream_t stream) {
   if (nred < 1 || nred > NCA_MAX_REDUCTIONS) fail(NCA_ERR_LIMIT, "%d reductions (1..%d)", nred, NCA_MAX_REDUCTIONS);
@@ -1840,7 +1860,51 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   const int64_t KG = KN / sp.vec;
   // one launch (plus its finalize) with `unroll` rows per thread in flight and
   // splits chosen for `tps` threads per SM
+  // the row-lane form applies with one reduced dim, no pointer axes and no IDX
+  int nrd = 0, rdim = -1;
+  for (int d = 0; d < s.nd; ++d) if (s.red[d]) { ++nrd; rdim = d; }
+  const bool rows_ok = nrd == 1 && sp.ptrmask == 0 && !tape.uses_idx && RN > 0;
+  // row-lane form: 4 row lanes per warp, 64 kept groups per CTA; splits for
+  // `tps` threads per SM with at least 8 rows per row lane
+  auto run_k4r = [&](int unroll, int tps, int lastcta) {
+    const int R = 4, GPC = (32 / R) * 8;
+    sp.unroll = unroll;
+    sp.k4r = R;
+    sp.rd = rdim;
+    const int64_t nset = cdiv(KG, GPC);
+    const int64_t target = (int64_t)sms * tps;
+    int64_t S = std::max<int64_t>(1, std::min<int64_t>(cdiv(target, nset * 256), RN / (8 * R)));
+    int64_t C = cdiv(RN, S);
+    S = cdiv(RN, C);
+    const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
+    std::vector<uint64_t> w;
+    fill_common_words(s, sp, tape, L, w);
+    w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+    sp.lastcta = (lastcta && S > 1) ? 1 : 0;
+    const size_t pbytes = S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0;
+    const size_t cbytes = sp.lastcta ? ((size_t)nset * 4 + 255) / 256 * 256 : 0;
+    StreamScratch part(pbytes + cbytes, stream);
+    if (S > 1) {
+      uint64_t* p = (uint64_t*)part.ptr;
+      if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
+      if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+      if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+      if (sp.lastcta) {
+        w[L.aux] = (uint64_t)(uintptr_t)p;
+        check_cuda(cudaMemsetAsync(p, 0, cbytes, stream), "arrival counters");
+      }
+    }
+    CUfunction fn = kernel_for(sp, tape);
+    launch(fn, nset * S, w, stream);
+    if (S > 1 && !sp.lastcta) launch_finalize(sp, tape, KN, S, sms, w, stream);
+    sp.k4r = 0;
+    sp.rd = 0;
+  };
   auto run_k4 = [&](int unroll, int tps, int lastcta) {
+    if (unroll >= 100) {   // the row-lane form: unroll - 100 rows in flight
+      run_k4r(unroll - 100, tps, lastcta);
+      return;
+    }
     sp.unroll = unroll;
     const int64_t target = (int64_t)sms * tps;
     int64_t S = 1;
@@ -1883,7 +1947,8 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   for (int k = 0; k < nops; ++k) key += std::to_string(ops[k].dtype) + ".";
   key += "|r" + size_class(RN) + "|k" + size_class(KN) + "|d" + std::to_string(s.nd) + "|v" + std::to_string(sp.vec);
   std::vector<int> choice;
-  if (tune_get(key, choice) && choice.size() == 3 && (choice[0] == 4 || choice[0] == 8) &&
+  if (tune_get(key, choice) && choice.size() == 3 &&
+      (choice[0] == 4 || choice[0] == 8 || (rows_ok && (choice[0] == 102 || choice[0] == 104))) &&
       (choice[1] == 512 || choice[1] == 1024 || choice[1] == 2048) && (choice[2] == 0 || choice[2] == 1)) {
     run_k4(choice[0], choice[1], choice[2]);
     return;
@@ -1892,8 +1957,11 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   for (int k = 0; k < nred; ++k) routs.push_back(rv[(size_t)k].out);
   if (out) routs.push_back(*out);
   if (KN * RN >= (1 << 16) && tune_should_search(stream) && rerun_safe(ops, nops, routs.data(), (int)routs.size())) {
-    const std::vector<std::vector<int>> cands = {{4, 1024, 0}, {8, 1024, 0}, {4, 2048, 0}, {8, 2048, 0}, {8, 512, 0},
-                                                 {4, 1024, 1}, {8, 512, 1}};
+    std::vector<std::vector<int>> cands = {{4, 1024, 0}, {8, 1024, 0}, {4, 2048, 0}, {8, 2048, 0}, {8, 512, 0},
+                                           {4, 1024, 1}, {8, 512, 1}};
+    if (rows_ok)
+      for (auto c : std::vector<std::vector<int>>{{104, 2048, 1}, {104, 2048, 0}, {102, 2048, 1}, {104, 1024, 1}})
+        cands.push_back(c);
     const int best = tune_pick(stream, (int)cands.size(), [&](int i) {
       run_k4(cands[(size_t)i][0], cands[(size_t)i][1], cands[(size_t)i][2]);
     });
@@ -1901,7 +1969,8 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     run_k4(cands[(size_t)best][0], cands[(size_t)best][1], cands[(size_t)best][2]);
     return;
   }
-  run_k4(4, 1024, 0);
+  if (rows_ok && !k4r_off()) run_k4(104, 1024, k4r_lastcta());
+  else run_k4(4, 1024, 0);
 }
 
 }  // namespace nca
@@ -1963,6 +2032,12 @@ int jit_selftest(const char* arch) {
         Spec s3 = sp;
         s3.lastcta = 1;
         nvrtc_compile(gen_source(s3, t), a);
+        ++n;
+      }
+      if (kind == 4) {                 // row-lane form over the one reduced dim 1
+        Spec s4 = sp;
+        s4.k4r = 4; s4.rd = 1; s4.lastcta = 1; s4.unroll = 4;
+        nvrtc_compile(gen_source(s4, t), a);
         ++n;
       }
     }

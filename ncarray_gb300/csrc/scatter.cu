@@ -14,7 +14,9 @@
 //     warp instead of one per element);
 //   - privatises the destination in shared memory when it is small next to the
 //     input (each CTA accumulates its grid-stride share there and adds the
-//     non-zero entries to the destination once).
+//     non-zero entries to the destination once);
+//   - in the common case (1-D views, source of the destination's type) keeps
+//     four index and four source loads in flight per thread.
 // Integer destinations wrap (two's complement) exactly as the reference's
 // `+=` does. Floating destinations add in the order the atomics land, so the
 // result equals the reference's sequential sum up to rounding (the order of a
@@ -169,6 +171,84 @@ __global__ void __launch_bounds__(THREADS) scatter_add_kernel(ScatterArgs a) {
   }
 }
 
+// The common case in one pass with more loads in flight: 1-D views, the
+// source already of the destination's type, indices of 32 or 64 bits, a
+// destination below 2^31 entries (32-bit match keys). A warp takes 32 * U
+// consecutive elements per trip (U loads of each array in flight per thread,
+// the source loaded without waiting for its index); grouping and atomics as
+// in scatter_add_kernel.
+constexpr int U = 4;
+
+template <class D, class IW, bool SMEM>
+__global__ void __launch_bounds__(THREADS) scatter_fast_kernel(ScatterArgs a, int idx_signed) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  D* priv = reinterpret_cast<D*>(sm_raw);
+  if (SMEM) {
+    for (long long b = threadIdx.x; b < a.dest_n; b += THREADS) priv[b] = D(0);
+    __syncthreads();
+  }
+  const IW* idx = reinterpret_cast<const IW*>(a.idx);
+  const D* src = reinterpret_cast<const D*>(a.src);
+  const long long ist = a.istr[0] / (long long)sizeof(IW), sst = a.sstr[0] / (long long)sizeof(D);
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * THREADS * U;
+  for (long long base = ((long long)blockIdx.x * THREADS + (threadIdx.x & ~31)) * U; base < a.n; base += stride) {
+    IW raw[U];
+    D v[U];
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      const long long i = base + k * 32 + lane;
+      raw[k] = (IW)0;
+      v[k] = D(0);
+      if (i < a.n) {
+        raw[k] = idx[i * ist];
+        v[k] = src[i * sst];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < U; ++k) {
+      long long t;
+      if (sizeof(IW) == 4) t = idx_signed ? (long long)(int)(unsigned)raw[k] : (long long)(unsigned)raw[k];
+      else t = (long long)(unsigned long long)raw[k];   // uint64 >= 2^63 reads negative: dropped
+      if (base + k * 32 + lane >= a.n) t = -1;
+      const bool ok = t >= 0 && t < a.dest_n;
+      const unsigned key = ok ? (unsigned)t : 0x80000000u + (unsigned)lane;   // invalid lanes stay alone
+      const unsigned peers = __match_any_sync(0xffffffffu, key);
+      D s = ok ? v[k] : D(0);
+      const unsigned above = peers & ~((2u << lane) - 1u);
+      int next = above ? __ffs(above) - 1 : lane;
+      bool has = above != 0;
+      if (__any_sync(0xffffffffu, has)) {
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+          const D ov = shfl(s, next);
+          const int onext = __shfl_sync(0xffffffffu, next, next);
+          const bool ohas = __shfl_sync(0xffffffffu, has, next);
+          if (has) { s += ov; next = onext; has = ohas; }
+        }
+      }
+      if (ok && (peers & ((1u << lane) - 1u)) == 0) {
+        if (SMEM) atomic_add<D>(priv + t, s);
+        else atomic_add<D>(reinterpret_cast<D*>(a.dest + t * a.dest_stride), s);
+      }
+    }
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (long long b = threadIdx.x; b < a.dest_n; b += THREADS) {
+      const D v = priv[b];
+      if (v != D(0)) atomic_add<D>(reinterpret_cast<D*>(a.dest + b * a.dest_stride), v);
+    }
+  }
+}
+
+// true when the source dtype loads as D directly (same size and kind)
+template <class D> constexpr bool same_src(int dt) {
+  return (sizeof(D) == 4 && (D)0.5 != 0 && dt == NCA_FLOAT32) || (sizeof(D) == 8 && (D)0.5 != 0 && dt == NCA_FLOAT64) ||
+         (sizeof(D) == 4 && (D)0.5 == 0 && (dt == NCA_INT32 || dt == NCA_UINT32)) ||
+         (sizeof(D) == 8 && (D)0.5 == 0 && (dt == NCA_INT64 || dt == NCA_UINT64));
+}
+
 bool index_dtype_ok(int dt) {
   return dt == NCA_INT32 || dt == NCA_UINT32 || dt == NCA_INT64 || dt == NCA_UINT64;
 }
@@ -183,7 +263,23 @@ void launch(ScatterArgs& a, cudaStream_t s) {
   // elements to add than destination entries to flush
   const long long priv_ctas = (long long)sms * 4;
   const bool smem = bytes <= SMEM_MAX_BYTES && a.n >= 4 * priv_ctas * a.dest_n;
-  if (smem) {
+  const int isz = (a.idx_dt == NCA_INT64 || a.idx_dt == NCA_UINT64) ? 8 : 4;
+  const bool fast = a.nd == 1 && same_src<D>(a.src_dt) && a.dest_n < (1ll << 31) &&
+                    a.istr[0] % isz == 0 && a.sstr[0] % (long long)sizeof(D) == 0 &&
+                    (uintptr_t)a.idx % isz == 0 && (uintptr_t)a.src % sizeof(D) == 0;
+  if (fast) {
+    const int sgn = a.idx_dt == NCA_INT32 ? 1 : 0;
+    long long fb = (a.n + (long long)THREADS * U - 1) / ((long long)THREADS * U);
+    if (smem) {
+      fb = std::min(fb, priv_ctas);
+      if (isz == 4) scatter_fast_kernel<D, unsigned, true><<<(unsigned)fb, THREADS, (size_t)bytes, s>>>(a, sgn);
+      else scatter_fast_kernel<D, unsigned long long, true><<<(unsigned)fb, THREADS, (size_t)bytes, s>>>(a, sgn);
+    } else {
+      fb = std::min(fb, (long long)sms * 8);
+      if (isz == 4) scatter_fast_kernel<D, unsigned, false><<<(unsigned)fb, THREADS, 0, s>>>(a, sgn);
+      else scatter_fast_kernel<D, unsigned long long, false><<<(unsigned)fb, THREADS, 0, s>>>(a, sgn);
+    }
+  } else if (smem) {
     blocks = std::min(blocks, priv_ctas);
     scatter_add_kernel<D, true><<<(unsigned)blocks, THREADS, (size_t)bytes, s>>>(a);
   } else {
