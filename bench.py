@@ -122,6 +122,11 @@ def c2_bytes(n: int) -> dict:
     return {"fused": fused, "int": intexpr, "step": step}
 
 
+# NCA_C2_STEP=forked runs the step as two calls (the fused expression and the
+# int32 expression on two forked streams) instead of one nca_expr_multi pass
+C2_FORKED = os.environ.get("NCA_C2_STEP", "") == "forked"
+
+
 class C2Step:
     """One step through the public API (lazy tape -> fused kernel) on device arrays."""
 
@@ -143,9 +148,17 @@ class C2Step:
     def intexpr(self):
         self.z_expr.evaluate(out=self.z)
 
+    def multi(self):
+        """Both expressions in one pass (nca_expr_multi): x and k read once."""
+        self.nca.evaluate_many([(self.y_expr, self.y), (self.z_expr, self.z)], reductions=self.red,
+                               red_out=[self.mx, self.am])
+
     def __call__(self):
-        self.fused()
-        self.intexpr()
+        if C2_FORKED:
+            self.fused()
+            self.intexpr()
+        else:
+            self.multi()
 
     def forked(self, torch, side):
         """The step with the two expressions on two streams (they share only the
@@ -658,10 +671,10 @@ def measure_c5(torch, nca, peak, n_arrays=20000):
 def profile_op(torch, nca, op: str, steps: int) -> None:
     """Runs one op `steps` times at the bench size, with no timing or JSON:
     the target of small, self-terminating profiler captures."""
-    if op in ("c2-fused", "c2-int"):
+    if op in ("c2-fused", "c2-int", "c2-multi"):
         x, v, k = c2_host()
         step = C2Step(nca, nca.NCDevArray.from_host(x), nca.NCDevArray.from_host(v), nca.NCDevArray.from_host(k))
-        fn = step.fused if op == "c2-fused" else step.intexpr
+        fn = {"c2-fused": step.fused, "c2-int": step.intexpr, "c2-multi": step.multi}[op]
     elif op in ("c3-7", "c3-27"):
         from ncarray_gb300.stencil import Stencil3D, laplacian7, laplacian27
         st = Stencil3D(laplacian7() if op == "c3-7" else laplacian27(), 0.1)
@@ -721,6 +734,35 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
         B = Batch(arrays)
         B.run(graph=False)
         fn = lambda: B.run(graph=False)  # noqa: E731
+    elif op == "c2-multi-small":
+        # the one-pass C2 step on half of the b axis: x (64,128,256,8), k (8,128,256,64)
+        # (x, k, y, z 64 MiB each, above L2), for full profiler captures
+        rng = np.random.default_rng(SEED + 12)
+        x = rng.standard_normal((64, 128, 256, 8), dtype=np.float32)
+        v = rng.standard_normal(128, dtype=np.float32)
+        k = rng.integers(-1000, 1001, (8, 128, 256, 64), dtype=np.int32)
+        dx, dv, dk = (nca.NCDevArray.from_host(a) for a in (x, v, k))
+        with nca.lazy_mode():
+            ye = dx.permute(3, 1, 2, 0) * dv.reshape(1, 128, 1, 1) + dk
+            ze = (dk * 3 + 7) % 11
+        y, z = nca.NCDevArray(ye.shape, ye.dtype), nca.NCDevArray(ze.shape, ze.dtype)
+        red = [(nca.RedOp.MAX, 2), (nca.RedOp.ARGMAX, 2)]
+        fn = lambda: nca.evaluate_many([(ye, y), (ze, z)], reductions=red)  # noqa: E731
+    elif op == "c1-variants":
+        # the C1 expression and its parts (x, a*b, sqrt(abs(c)), 0.5*a, all) on
+        # float64 (128,128,128), each with the axis-0 sum and max, the sum, the
+        # max: float64 instruction counts per part
+        rng = np.random.default_rng(SEED)
+        da, db, dc = (nca.NCDevArray.from_host(rng.uniform(-1, 1, (128, 128, 128))) for _ in range(3))
+        with nca.lazy_mode():
+            parts = [da._expr(), da * db, nca.sqrt(abs(dc)), 0.5 * da, da * db + nca.sqrt(abs(dc)) - 0.5 * da]
+        outs = [nca.NCDevArray(e.shape, e.dtype) for e in parts]
+        reds = ([(nca.RedOp.SUM, 0), (nca.RedOp.MAX, 0)], [(nca.RedOp.SUM, 0)], [(nca.RedOp.MAX, 0)])
+
+        def fn():
+            for e, o in zip(parts, outs):
+                for r in reds:
+                    e.evaluate(out=o, reductions=r)
     elif op == "c5-general-small":
         # the general batched form (any tapes and reductions) on 1,000 of the uneven arrays
         from ncarray_gb300.batch import BatchExpr
@@ -893,7 +935,7 @@ def main():
     torch.cuda.synchronize()
     per_step_launches = _lib.lib().nca_launch_count() - l0
     side = torch.cuda.Stream()
-    g_step = make_graph(torch, lambda: step.forked(torch, side))
+    g_step = make_graph(torch, (lambda: step.forked(torch, side)) if C2_FORKED else step.multi)
     g_fused = make_graph(torch, step.fused)
     g_int = make_graph(torch, step.intexpr)
     for _ in range(args.warmup):
@@ -917,15 +959,19 @@ def main():
         dist.barrier()
     ms_total = e0.elapsed_time(e1)
     launches = per_step_launches * args.steps
-    # per-kernel timing (dominant kernel = the fused pass) for the roofline
+    # per-kernel timing for the roofline: the dominant kernel is the one-pass
+    # kernel (the whole step) or, for the forked step, the fused pass
     ms_fused = time_events(torch, g_fused.replay, args.steps)
     ms_int = time_events(torch, g_int.replay, args.steps)
+    ms_dom = ms_fused if C2_FORKED else time_events(torch, g_step.replay, args.steps)
+    bytes_dom = by["fused"] if C2_FORKED else by["step"]
     clocks = sampler.stop()
     value, ms_step = job_throughput(ms_total, args.steps, world, by["step"],
                                     (lambda v: all_reduce_max(dist, torch, v, "cuda")) if dist else (lambda v: v))
     peak, peak_kind = peaks()
     fused_gbs = by["fused"] / (ms_fused * 1e-3) / 1e9
     int_gbs = by["int"] / (ms_int * 1e-3) / 1e9
+    dom_gbs = bytes_dom / (ms_dom * 1e-3) / 1e9
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -1023,8 +1069,12 @@ def main():
                         s_cmp.wait_event(ev_in[S][i])
                         if cross:
                             s_cmp.wait_event(ev_out[S][i])  # and its results in set S are on the host
-                        c["ye"].evaluate(out=c["y"], reductions=red, red_out=[c["mx"], c["am"]])
-                        c["ze"].evaluate(out=c["z"])
+                        if C2_FORKED:
+                            c["ye"].evaluate(out=c["y"], reductions=red, red_out=[c["mx"], c["am"]])
+                            c["ze"].evaluate(out=c["z"])
+                        else:
+                            nca.evaluate_many([(c["ye"], c["y"]), (c["ze"], c["z"])], reductions=red,
+                                              red_out=[c["mx"], c["am"]])
                         ev_cmp[S][i].record(s_cmp)
                     with torch.cuda.stream(s_out):
                         s_out.wait_event(ev_cmp[S][i])
@@ -1076,8 +1126,10 @@ def main():
         cpu = {"value": round(gbs, 3), "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"view slice 0 of 8 along axis 0 ({ns} elements), one step, {dt:.2f} s"}
 
-    per_op = {"c2_fused_expr_max_argmax": {"GB/s": round(fused_gbs, 1), "frac_of_measured": round(fused_gbs / peak, 4)},
-              "c2_int_expr": {"GB/s": round(int_gbs, 1), "frac_of_measured": round(int_gbs / peak, 4)}}
+    per_op = {"c2_fused_expr_max_argmax": {"GB/s": round(fused_gbs, 1), "frac_of_measured": round(fused_gbs / peak, 4),
+                                           "ms": round(ms_fused, 5), "note": "the first expression alone"},
+              "c2_int_expr": {"GB/s": round(int_gbs, 1), "frac_of_measured": round(int_gbs / peak, 4),
+                              "ms": round(ms_int, 5), "note": "the int32 expression alone"}}
     if not args.headline_only:
         del step, dx, dv, dk
         torch.cuda.empty_cache()
@@ -1097,7 +1149,7 @@ def main():
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        t = json.loads(tf.read_text()).get("c2_fused")
+        t = json.loads(tf.read_text()).get("c2_fused" if C2_FORKED else "c2_multi")
         if t:
             traffic = t.get("bytes_per_launch")
     line = {
@@ -1107,13 +1159,17 @@ def main():
         "config": {"workload": "strided/broadcast fusion: x f32 (64,256,256,8) viewed (3,1,2,0) * v[None,:,None,None]"
                                " + k i32 (8,256,256,64); y stored + max/argmax axis 2 in one pass; (k*3+7)%11",
                    "elements": n, "bytes_per_step": by["step"], "l2": "working set 640 MB > L2; no flush",
-                   "launch": "each step is one replay of a CUDA graph of its C-ABI calls (the fused and the "
-                             "int32 expressions on two forked streams)",
+                   "launch": ("each step is one replay of a CUDA graph of its C-ABI calls (the fused and the "
+                              "int32 expressions on two forked streams)") if C2_FORKED else
+                             ("each step is one replay of a CUDA graph of one nca_expr_multi call: y, z, max and "
+                              "argmax from one TMA-staged pass that reads x and k once"),
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "achieved": round(fused_gbs, 2), "peak": peak, "unit": "GB/s",
-                     "frac": round(fused_gbs / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
-                     "kernel": "nca_staged_async: TMA-staged fused expression + axis-2 max/argmax",
-                     "bytes_per_launch": by["fused"], "ms_per_launch": round(ms_fused, 5)},
+        "roofline": {"bound": "hbm", "achieved": round(dom_gbs, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(dom_gbs / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                     "kernel": ("nca_staged_async: TMA-staged fused expression + axis-2 max/argmax") if C2_FORKED else
+                               ("nca_staged_async with an extra output: y = x.permute * v + k stored, max/argmax "
+                                "over axis 2, z = (k*3+7)%11 stored, one pass"),
+                     "bytes_per_launch": bytes_dom, "ms_per_launch": round(ms_dom, 5)},
         "per_op": per_op,
         "gpu_launches": int(launches),
         "clocks": clocks,

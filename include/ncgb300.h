@@ -193,6 +193,20 @@ int32_t nca_expr_reduce(const nca_tape* tape, const nca_view* operands, int32_t 
                         const nca_view* expr_out, const nca_reduction* reds,
                         int32_t n_reds, void* stream);
 
+/* Several expressions over the same operands in one pass. tapes[0] is
+ * evaluated, stored to outs[0] and reduced by reds (as nca_expr_reduce;
+ * n_reds may be 0), and each further tape i over the same operands is stored
+ * elementwise to outs[i] (outs[0]'s shape), with the results of running
+ * nca_expr_reduce and then nca_expr_eval for each further tape in order.
+ * The pass reads every operand once when the views allow it (transposed
+ * operands staged by TMA, 4-byte outputs) and no output overlaps an operand or
+ * another output; otherwise the calls run one after another. No reference
+ * counterpart: ncarray evaluates each expression in a GPUEngine call of its
+ * own (engines/gpuengine.hh:90-195). */
+#define NCA_MAX_EXTRA_OUTS 3
+int32_t nca_expr_multi(const nca_tape* tapes, int32_t n_tapes, const nca_view* operands, int32_t n_operands,
+                       const nca_view* outs, const nca_reduction* reds, int32_t n_reds, void* stream);
+
 /* Reduction of one view: GPUEngine::execute_reduce_axes (gpuengine.hh:222-288)
  * when axes_mask is partial, GPUEngine::execute_full_reduce (:301-333) when it
  * covers every axis. */

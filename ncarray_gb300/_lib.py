@@ -91,6 +91,8 @@ EXPORTS = {
     "nca_jit_selftest": (c_int32, [c_char_p, POINTER(c_int32)]),
     "nca_expr_eval": (c_int32, [POINTER(Tape), POINTER(View), c_int32, POINTER(View), c_void_p]),
     "nca_expr_reduce": (c_int32, [POINTER(Tape), POINTER(View), c_int32, POINTER(View), POINTER(Reduction), c_int32, c_void_p]),
+    "nca_expr_multi": (c_int32, [POINTER(Tape), c_int32, POINTER(View), c_int32, POINTER(View), POINTER(Reduction),
+                                 c_int32, c_void_p]),
     "nca_reduce": (c_int32, [POINTER(View), c_int32, c_uint32, POINTER(View), c_void_p]),
     "nca_reduce_noalloc": (c_int32, [POINTER(View), c_int32, POINTER(View), c_void_p]),
     "nca_copy": (c_int32, [POINTER(View), POINTER(View), c_void_p]),

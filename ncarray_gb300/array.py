@@ -571,27 +571,8 @@ class DevExpr:
                 _lib.call("nca_expr_eval", ctypes.byref(t), ops, n, ctypes.byref(out.view_struct()), stream)
             return []
         shape = out.shape if out is not None else self.shape
-        results, rs = [], []
-        for i, (op, axes) in enumerate(reductions):
-            op = RedOp(op)
-            mask, kept = _axes_mask(axes, len(shape))
-            odt = _red_out_dtype(op, self.expr_dtype)
-            if red_out is not None:
-                res = red_out[i]
-                if res.dtype != odt or res.shape != tuple(shape[d] for d in kept):
-                    raise ValueError(f"reduction output {i} must be {odt.name} {[shape[d] for d in kept]}")
-            else:
-                res = NCDevArray([shape[d] for d in kept], odt)
-            results.append(res)
-            r = _lib.Reduction()
-            r.op = int(op)
-            r.axes_mask = mask
-            r.out = res.view_struct()
-            rs.append(r)
-        masks = {r.axes_mask for r in rs}
-        if len(masks) != 1:
-            raise ValueError("one evaluate() call reduces over one set of axes")
-        rarr = (_lib.Reduction * len(rs))(*rs)
+        results, rarr = _reductions(shape, self.expr_dtype, reductions, red_out)
+        rs = list(rarr)
         if out is not None and out.size == 0:
             out = None
         _lib.call("nca_expr_reduce", ctypes.byref(t), ops, n,
@@ -658,6 +639,78 @@ class DevExpr:
 
     def argmin(self, axes=None):
         return self._reduce(RedOp.ARGMIN, axes)
+
+
+def _reductions(shape, expr_dtype: DType, reductions, red_out):
+    """The result arrays of (RedOp, axes) reductions of a value of `shape` and
+    their C descriptors (one shared axes mask)."""
+    results, rs = [], []
+    for i, (op, axes) in enumerate(reductions):
+        op = RedOp(op)
+        mask, kept = _axes_mask(axes, len(shape))
+        odt = _red_out_dtype(op, expr_dtype)
+        if red_out is not None:
+            res = red_out[i]
+            if res.dtype != odt or res.shape != tuple(shape[d] for d in kept):
+                raise ValueError(f"reduction output {i} must be {odt.name} {[shape[d] for d in kept]}")
+        else:
+            res = NCDevArray([shape[d] for d in kept], odt)
+        results.append(res)
+        r = _lib.Reduction()
+        r.op = int(op)
+        r.axes_mask = mask
+        r.out = res.view_struct()
+        rs.append(r)
+    if len({r.axes_mask for r in rs}) > 1:
+        raise ValueError("one evaluate() call reduces over one set of axes")
+    return results, (_lib.Reduction * max(len(rs), 1))(*rs)
+
+
+def evaluate_many(outputs, reductions: Iterable = (), red_out=None):
+    """Several expressions over shared operands in one pass (nca_expr_multi).
+
+    `outputs` is a list of (expression, out array) pairs, all of one shape; the
+    reductions (as in DevExpr.evaluate) apply to the first expression. The
+    results equal evaluating the first expression with its reductions and then
+    each further expression into its array; when the views allow it (operands
+    staged by TMA, 4-byte outputs, no output overlapping an operand or another
+    output) every operand is read once for all of them. Returns the reduction
+    results."""
+    outputs = list(outputs)
+    if not outputs:
+        raise ValueError("nothing to evaluate")
+    exprs = [_as_node(e) for e, _ in outputs]
+    outs = [o for _, o in outputs]
+    shape = outs[0].shape
+    for e, o in zip(exprs, outs):
+        if o.shape != shape or e.shape != shape:
+            raise ValueError("every expression and output must have the first output's shape")
+    # one operand list: equal views become one operand, the tapes' loads are renumbered
+    arrays, index = [], {}
+    tapes = []
+    for e in exprs:
+        remap = []
+        for a in e.arrays:
+            k = _view_key(a)
+            if k not in index:
+                index[k] = len(arrays)
+                arrays.append(a)
+            remap.append(index[k])
+        if remap != list(range(len(remap))):
+            r = DevExpr()
+            r.arrays, r.scalars, r.work, r.expr_dtype = [arrays[j] for j in remap], e.scalars, e.work, e.expr_dtype
+            r.instrs = [((ins >> 24) << 24) | remap[ins & 0xFFFFFF]
+                        if (ins >> 24) in (OpCode.LOAD_NCARR, OpCode.LOAD_SOARR) else ins for ins in e.instrs]
+            e = r
+        tapes.append(e._tape())
+    reductions = list(reductions)
+    results, rarr = _reductions(shape, exprs[0].expr_dtype, reductions, red_out)
+    tarr = (_lib.Tape * len(tapes))(*[t for t, _ in tapes])
+    ops = (_lib.View * max(len(arrays), 1))(*[a.view_struct() for a in arrays])
+    oarr = (_lib.View * len(outs))(*[o.view_struct() for o in outs])
+    if all(o.size for o in outs):
+        _lib.call("nca_expr_multi", tarr, len(tapes), ops, len(arrays), oarr, rarr, len(reductions), current_stream())
+    return results
 
 
 def _view_key(a: NCDevArray):

@@ -70,6 +70,19 @@ int32_t nca_expr_reduce(const nca_tape* tape, const nca_view* operands, int32_t 
   });
 }
 
+int32_t nca_expr_multi(const nca_tape* tapes, int32_t n_tapes, const nca_view* operands, int32_t n_operands,
+                       const nca_view* outs, const nca_reduction* reds, int32_t n_reds, void* stream) {
+  return guarded([&] {
+    if (!tapes || !outs) fail(NCA_ERR_INVALID, "null tapes or outputs");
+    if (n_tapes < 1) fail(NCA_ERR_INVALID, "at least one tape");
+    if (n_reds > 0 && !reds) fail(NCA_ERR_INVALID, "null reductions");
+    if (n_operands > 0 && !operands) fail(NCA_ERR_INVALID, "null operands");
+    std::vector<Tape> ts;
+    for (int i = 0; i < n_tapes; ++i) ts.push_back(make_tape(&tapes[i], n_operands));
+    expr_multi(ts, operands, n_operands, outs, reds, n_reds, (cudaStream_t)stream);
+  });
+}
+
 // identity tape over one view: LOAD_NCARR 0
 static nca_tape identity_tape(int dt, uint32_t* instr) {
   nca_tape t;

@@ -183,6 +183,7 @@ struct Space {
   bool has_out = false;
   CArr out;
   std::vector<CArr> reds;
+  std::vector<CArr> xouts;   // extra outputs (other tapes over the same operands, out's shape)
   int64_t total() const { int64_t t = 1; for (int d = 0; d < nd; ++d) t *= shape[d]; return t; }
 };
 
@@ -210,7 +211,8 @@ static const char* view_base(const nca_view& v) {
 
 // Builds the logical-order space (size-1 dims dropped). `lshape` has n dims.
 static Space make_space(const int64_t* lshape, int n, const nca_view* ops, int nops,
-                        const nca_view* out, uint32_t red_mask, const nca_reduction* reds, int nred) {
+                        const nca_view* out, uint32_t red_mask, const nca_reduction* reds, int nred,
+                        const nca_view* xouts = nullptr, int nx = 0) {
   Space s;
   for (int k = 0; k < nops; ++k) {
     CArr a; a.dtype = ops[k].dtype;
@@ -240,6 +242,9 @@ static Space make_space(const int64_t* lshape, int n, const nca_view* ops, int n
   for (int k = 0; k < nred; ++k) {
     CArr a; a.base = view_base(reds[k].out); a.dtype = reds[k].out.dtype; s.reds.push_back(a);
   }
+  for (int k = 0; k < nx; ++k) {
+    CArr a; a.base = view_base(xouts[k]); a.dtype = xouts[k].dtype; s.xouts.push_back(a);
+  }
   int kept_pos = 0;
   for (int d = 0; d < n; ++d) {
     const bool is_red = (red_mask >> d) & 1u;
@@ -263,6 +268,7 @@ static Space make_space(const int64_t* lshape, int n, const nca_view* ops, int n
     }
     if (out) s.out.st[c] = out->strides[d];
     for (int k = 0; k < nred; ++k) s.reds[k].st[c] = is_red ? 0 : reds[k].out.strides[kd];
+    for (int k = 0; k < nx; ++k) s.xouts[k].st[c] = xouts[k].strides[d];
   }
   return s;
 }
@@ -275,6 +281,7 @@ static bool mergeable(const Space& s, int i) {  // dims i (outer) and i+1 (inner
   for (auto& a : s.ops) if (!ok(a)) return false;
   if (s.has_out && !ok(s.out)) return false;
   for (auto& a : s.reds) if (!ok(a)) return false;
+  for (auto& a : s.xouts) if (!ok(a)) return false;
   return true;
 }
 
@@ -290,6 +297,7 @@ static void merge_dims(Space& s) {
     for (auto& a : s.ops) fold(a);
     if (s.has_out) fold(s.out);
     for (auto& a : s.reds) fold(a);
+    for (auto& a : s.xouts) fold(a);
     for (int d = i + 1; d + 1 < s.nd; ++d) { s.shape[d] = s.shape[d + 1]; s.red[d] = s.red[d + 1]; }
     --s.nd;
   }
@@ -306,6 +314,7 @@ static void permute_dims(Space& s, const std::vector<int>& perm) {
     }
     if (s.has_out) t.out.st[c] = s.out.st[perm[c]];
     for (size_t k = 0; k < s.reds.size(); ++k) t.reds[k].st[c] = s.reds[k].st[perm[c]];
+    for (size_t k = 0; k < s.xouts.size(); ++k) t.xouts[k].st[c] = s.xouts[k].st[perm[c]];
   }
   s = t;
 }
@@ -354,6 +363,10 @@ struct Spec {
   int block = 256;   // kinds 1, 2: threads per block (NCA_LB)
   int k4r = 0;       // kind 4: row lanes per warp (row-lane form, one reduced dim rd); 0: thread per column group
   int rd = 0;
+  // kind 7: extra outputs, each a tape over the same operands stored elementwise
+  std::vector<Tape> xtapes;
+  std::vector<int> xout_dtypes;
+  int xvec = 0;   // the extra tapes read only p-row and uniform operands: 16 bytes of a tile at a time
 };
 
 struct WordLayout {
@@ -468,34 +481,71 @@ static std::string vec_type(int bytes) {
 
 // The tape as statements over the compute type nca_w ending in `return`;
 // operand k is loaded as load_prefix + k + load_suffix.
+// The tape as a C++ function body over the loaded operands (`load_prefix` k
+// `load_suffix`), computing in the type named `W` (nca_w, or nca_wx<i> for an
+// extra output's tape) with its scalars from s[sbase + i].
+// An integer division or remainder by a tape constant takes the constant as a
+// literal (the compiler then divides by multiplication); the kernel cache key
+// holds the constants of integer tapes (literal_key).
+static std::string int_literal(const Tape& t, int idx) {
+  const int wdt = arith_dtype(t.compute_dtype);
+  const uint64_t w = scalar_word(wdt, t.scalar_dtypes[(size_t)idx], t.scalar_slots[(size_t)idx]);
+  const int sz = dtinfo(wdt).size;
+  const uint64_t m = sz >= 8 ? ~0ull : ((1ull << (8 * sz)) - 1);
+  const uint64_t u = w & m;
+  if (dtinfo(wdt).is_signed) {
+    const int64_t v = sz >= 8 ? (int64_t)u : (int64_t)(u ^ (1ull << (8 * sz - 1))) - (int64_t)(1ull << (8 * sz - 1));
+    return "(" + std::to_string(v) + "ll)";
+  }
+  return "(" + std::to_string(u) + "ull)";
+}
+static bool literal_divisors(const Tape& t) {
+  const int wdt = arith_dtype(t.compute_dtype);
+  return !dtinfo(wdt).is_float && wdt != NCA_BOOL;
+}
+static std::string literal_key(const Tape& t) {
+  std::string k;
+  if (!literal_divisors(t)) return k;
+  for (size_t i = 0; i < t.scalar_slots.size(); ++i) k += std::to_string(t.scalar_slots[i]) + ",";
+  return k;
+}
+
 static std::string gen_eval(const Tape& t, const std::string& load_prefix = "v[",
-                            const std::string& load_suffix = "][q]") {
+                            const std::string& load_suffix = "][q]", const std::string& W = "nca_w",
+                            int sbase = 0) {
   std::ostringstream os;
-  std::vector<std::string> st;
+  const bool lit = literal_divisors(t);
+  struct Ent { std::string e, lit; };   // an expression and, for an integer constant, its literal
+  std::vector<Ent> st;
   int tmp = 0;
-  const std::string W = "nca_w";
+  auto pop = [&]() { Ent x = st.back(); st.pop_back(); return x; };
   for (uint32_t ins : t.instrs) {
     const int op = (int)(ins >> 24), idx = (int)(ins & 0xffffff);
     auto push_tmp = [&](const std::string& e) {
       const std::string n = "t" + std::to_string(tmp++);
-      os << "  const nca_w " << n << " = " << e << ";\n";
-      st.push_back(n);
+      os << "  const " << W << " " << n << " = " << e << ";\n";
+      st.push_back({n, ""});
     };
     switch (op) {
       case NCA_OP_NOOP: break;
-      case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR: st.push_back(load_prefix + std::to_string(idx) + load_suffix); break;
-      case NCA_OP_LOAD_CONST: st.push_back("nca_word<nca_w>(s[" + std::to_string(idx) + "])"); break;
-      case NCA_OP_IDX: push_tmp("(nca_w)lin"); break;
+      case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR:
+        st.push_back({load_prefix + std::to_string(idx) + load_suffix, ""});
+        break;
+      case NCA_OP_LOAD_CONST:
+        st.push_back({"nca_word<" + W + ">(s[" + std::to_string(idx + sbase) + "])", lit ? int_literal(t, idx) : ""});
+        break;
+      case NCA_OP_IDX: push_tmp("(" + W + ")lin"); break;
       default: {
         const int ar = op_arity(op);
         if (ar == A_UNARY) {
-          const std::string a = st.back(); st.pop_back();
+          const std::string a = pop().e;
           const char* f = op == NCA_OP_NEG ? "nca_neg" : op == NCA_OP_INC ? "nca_inc" : op == NCA_OP_DEC ? "nca_dec"
                         : op == NCA_OP_LNOT ? "nca_lnot" : op == NCA_OP_BNOT ? "nca_bnot" : op == NCA_OP_ABS ? "nca_abs" : "nca_sqrt";
-          push_tmp(std::string(f) + "<nca_w>(" + a + ")");
+          push_tmp(std::string(f) + "<" + W + ">(" + a + ")");
         } else {
-          const std::string b = st.back(); st.pop_back();
-          const std::string a = st.back(); st.pop_back();
+          const Ent eb = pop(), ea = pop();
+          const std::string& a = ea.e;
+          const std::string& b = eb.e;
           const char* f = nullptr;
           switch (op) {
             case NCA_OP_ADD: f = "nca_add"; break; case NCA_OP_SUB: f = "nca_sub"; break;
@@ -508,19 +558,21 @@ static std::string gen_eval(const Tape& t, const std::string& load_prefix = "v["
             case NCA_OP_BOR: f = "nca_bor"; break; case NCA_OP_XOR: f = "nca_xor"; break;
             default: fail(NCA_ERR_UNSUPPORTED, "opcode %d", op);
           }
-          // a multiplication by a tape constant (power-of-two constants
-          // scale exactly on the integer pipe for float64)
           const bool ca = a.rfind("nca_word<", 0) == 0, cb = b.rfind("nca_word<", 0) == 0;
-          if (op == NCA_OP_MUL && (ca != cb))
-            push_tmp("nca_mulc<nca_w>(" + (cb ? a : b) + ", " + (cb ? b : a) + ")");
+          if (!eb.lit.empty() && (op == NCA_OP_DIV || op == NCA_OP_MOD))
+            // an integer divisor known when the kernel is compiled
+            push_tmp(std::string(f) + "<" + W + ">(" + a + ", (" + W + ")" + eb.lit + ")");
+          else if (op == NCA_OP_MUL && (ca != cb))
+            // a multiplication by a tape constant (power-of-two constants
+            // scale exactly on the integer pipe for float64)
+            push_tmp("nca_mulc<" + W + ">(" + (cb ? a : b) + ", " + (cb ? b : a) + ")");
           else
-            push_tmp(std::string(f) + "<nca_w>(" + a + ", " + b + ")");
+            push_tmp(std::string(f) + "<" + W + ">(" + a + ", " + b + ")");
         }
       }
     }
   }
-  std::string res = st.back();
-  return os.str() + "  return " + res + ";\n";
+  return os.str() + "  return " + st.back().e + ";\n";
 }
 
 const char* jit_ctype(int dtype) { return dtinfo(arith_dtype(dtype)).ctype; }
@@ -696,6 +748,67 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
   os << "__device__ __forceinline__ nca_w nca_eval(const nca_w (*v)[NCA_VEC], int q, const u64* s, i64 lin) {\n"
      << "  (void)v; (void)q; (void)s; (void)lin;\n"
      << gen_eval(t) << "}\n";
+  // extra outputs (kind 7): per tape its compute type, operand loads, value
+  // and store; nca_xouts evaluates every extra tape at one element from the
+  // operands' addresses and stores it to its output slot
+  os << "#define NCA_NX " << sp.xtapes.size() << "\n";
+  if (!sp.xtapes.empty()) {
+    int sbase = (int)t.scalar_dtypes.size();
+    std::ostringstream xo, xv;
+    xo << "__device__ __forceinline__ void nca_xouts(const char* const* ap, const u64* s, char* const* op) {\n"
+       << "  (void)ap; (void)s;\n";
+    for (size_t x = 0; x < sp.xtapes.size(); ++x) {
+      const Tape& xt = sp.xtapes[x];
+      const std::string W = "nca_wx" + std::to_string(x);
+      os << "typedef " << dtinfo(xt.compute_dtype).ctype << " " << W << ";\n";
+      os << "__device__ __forceinline__ " << W << " nca_evalx" << x << "(const " << W << " (*v)[1], const u64* s) {\n"
+         << "  (void)v; (void)s; const i64 lin = 0; (void)lin;\n"
+         << gen_eval(xt, "v[", "][0]", W, sbase) << "}\n";
+      const int dt = sp.xout_dtypes[x];
+      const int es = dtinfo(dt).size;
+      os << "__device__ __forceinline__ void nca_putx" << x << "(char* p, " << W << " e) { *(" << storage_uint(es)
+         << "*)p = (" << storage_uint(es) << ")" << to_bits(dt, "e") << "; }\n";
+      // loads of the operands this tape reads, converted to its compute type
+      std::vector<bool> used(sp.nops, false);
+      for (uint32_t ins : xt.instrs) {
+        const int op = (int)(ins >> 24), idx = (int)(ins & 0xffffff);
+        if ((op == NCA_OP_LOAD_NCARR || op == NCA_OP_LOAD_SOARR) && idx < sp.nops) used[idx] = true;
+      }
+      xo << "  {\n    " << W << " v[" << std::max(sp.nops, 1) << "][1];\n";
+      for (int k = 0; k < sp.nops; ++k) {
+        if (!used[k]) continue;
+        const int odt = sp.op_dtypes[k];
+        xo << "    v[" << k << "][0] = (" << W << ")(" << from_bits(odt, "*(const " + storage_uint(dtinfo(odt).size) +
+              "*)(ap[" + std::to_string(k) + "])") << ");\n";
+      }
+      xo << "    nca_putx" << x << "(op[" << x << "], nca_evalx" << x << "(v, s));\n  }\n";
+      // four consecutive elements: p-row operands 16 bytes at ap[k], uniform
+      // operands one value at ap[k] (kind 7 operands and outputs are 4 bytes)
+      xv << "  {\n    " << W << " v[" << std::max(sp.nops, 1) << "][1];\n    uint4 o;\n";
+      for (int j = 0; j < 4; ++j) {
+        for (int k = 0; k < sp.nops; ++k) {
+          if (!used[k]) continue;
+          const int odt = sp.op_dtypes[k];
+          const bool prow = ((sp.pmask >> k) & 1u) != 0;
+          const std::string src = prow ? "u" + std::to_string(k) + "." + kWordNames[j] : "*(const u32*)(ap[" + std::to_string(k) + "])";
+          xv << "    v[" << k << "][0] = (" << W << ")(" << from_bits(odt, "(" + storage_uint(4) + ")(" + src + ")") << ");\n";
+        }
+        xv << "    o." << kWordNames[j] << " = (u32)" << to_bits(dt, "nca_evalx" + std::to_string(x) + "(v, s)") << ";\n";
+      }
+      xv << "    *(uint4*)op[" << x << "] = o;\n  }\n";
+      sbase += (int)xt.scalar_dtypes.size();
+    }
+    xo << "}\n";
+    os << xo.str();
+    if (sp.xvec) {
+      os << "__device__ __forceinline__ void nca_xouts4(const char* const* ap, const u64* s, char* const* op) {\n"
+         << "  (void)ap; (void)s;\n";
+      for (int k = 0; k < sp.nops; ++k)
+        if ((sp.pmask >> k) & 1u) os << "  const uint4 u" << k << " = *(const uint4*)(ap[" << k << "]);\n";
+      os << xv.str() << "}\n";
+    }
+  }
+  os << "#define NCA_XVEC " << sp.xvec << "\n";
 
   // ---- stores ----
   if (sp.has_out) {
@@ -977,6 +1090,15 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
   add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
   add(sp.nob); add(sp.lastcta); add(sp.block); add(sp.k4r); add(sp.rd);
+  k += literal_key(t) + '|';
+  add(sp.xvec);
+  for (size_t x = 0; x < sp.xtapes.size(); ++x) {
+    k += 'X';
+    add(sp.xtapes[x].compute_dtype); add(sp.xout_dtypes[x]);
+    for (uint32_t i : sp.xtapes[x].instrs) add(i);
+    for (int d : sp.xtapes[x].scalar_dtypes) add(d);
+    k += literal_key(sp.xtapes[x]);
+  }
   for (int d : sp.op_dtypes) add(d);
   k += '|';
   for (int m : sp.op_modes) add(m);
@@ -1130,7 +1252,13 @@ static void fill_common_words(const Space& s, const Spec& sp, const Tape& t, con
     for (int d = 0; d < sp.nd; ++d) w[L.outs + d] = (uint64_t)s.out.st[d];
   }
   for (int d = 0; d < sp.nd; ++d) w[L.shape + d] = (uint64_t)s.shape[d];
-  for (int i = 0; i < sp.nscal; ++i) w[L.scal + i] = scalar_word(sp.w, t.scalar_dtypes[i], t.scalar_slots[i]);
+  // the tape's scalars, then each extra output tape's (in its compute dtype)
+  int si = 0;
+  for (size_t i = 0; i < t.scalar_dtypes.size() && si < sp.nscal; ++i, ++si)
+    w[L.scal + si] = scalar_word(sp.w, t.scalar_dtypes[i], t.scalar_slots[i]);
+  for (const Tape& xt : sp.xtapes)
+    for (size_t i = 0; i < xt.scalar_dtypes.size() && si < sp.nscal; ++i, ++si)
+      w[L.scal + si] = scalar_word(xt.compute_dtype, xt.scalar_dtypes[i], xt.scalar_slots[i]);
   for (int k = 0; k < sp.nred; ++k) {
     w[L.redb + k] = (uint64_t)(uintptr_t)s.reds[k].base;
     for (int d = 0; d < sp.nd; ++d) w[L.reds + k * sp.nd + d] = (uint64_t)s.reds[k].st[d];
@@ -1311,13 +1439,20 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
     }
   }
   if (sp.has_out && !tma_ok(s.out, false)) return false;
+  const int nx = (int)sp.xtapes.size();
+  if (nx > 0 && !sp.has_out) return false;
+  for (const CArr& a : s.xouts)
+    if (dtinfo(a.dtype).size != 4 || !tma_ok(a, false)) return false;
   // block of rb loop indices: a divisor of the fastest loop extent whose
   // (loop index, q) rows fill whole 128-byte boxes, at most 128 of them, the
   // largest whose stages fit in the 227 KiB a CTA may use. 128 rows per block
   // and 2 stages measured best on the permuted (8,256,256,64) float32 views (about 97 KiB per CTA, two
   // CTAs per SM: 5.6 TB/s against 5.4 TB/s for 64 rows and 3 stages, three
   // CTAs per SM)
-  const int64_t budget = 227 * 1024;
+  // with extra outputs (one more output tile each) the block shrinks so that
+  // two CTAs still fit on an SM: (8, 256, 256, 64) with one extra output ran
+  // 4.96 TB/s at 64 rows, 3.66 TB/s at 128 rows (one CTA per SM)
+  const int64_t budget = sp.xtapes.empty() ? 227 * 1024 : 113 * 1024;
   const int tp = 32;
   int rb_max = (int)std::max<int64_t>(1, 128 / QX);
   if (const char* e = getenv("NCA_STAGED_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) rb_max = v; }
@@ -1329,7 +1464,7 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   auto smem_for = [&](int c, int n) {
     const int64_t rq = (int64_t)c * QX;
     const int64_t stage = nt * ((rq / 32) * tp * 128) + npc * (rq * 128);
-    return n * stage + nob * (rq * 128) + 16 * n + 16 * nob + 1024;
+    return n * stage + nob * (1 + nx) * (rq * 128) + 16 * n + 16 * nob + 1024;
   };
   int rb = 0, ns = 2;
   for (int c = 16; c >= 1 && rb == 0; c /= 2) {
@@ -1355,13 +1490,25 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   sp.qd = qd; sp.qx = (int)QX; sp.qxp = qxp; sp.tp = tp; sp.rb = rb; sp.tmask = tmask; sp.tile_bytes = 0;
   sp.ns = ns; sp.ld = ld; sp.npc = npc; sp.pmask = pmask; sp.umask = umask; sp.uumask = uumask; sp.ltp8 = 2;
   sp.nob = nob;
-  sp.nmaps = nt + npc + (sp.has_out ? 1 : 0);
+  sp.nmaps = nt + npc + (sp.has_out ? 1 + nx : 0);
+  // extra tapes over p-row and uniform operands only run on whole 16-byte
+  // chunks of the tiles (the p-row and output tiles share one layout)
+  sp.xvec = 0;
+  if (nx > 0) {
+    bool ok = true;
+    for (const Tape& xt : sp.xtapes)
+      for (uint32_t ins : xt.instrs) {
+        const int op = (int)(ins >> 24), idx = (int)(ins & 0xffffff);
+        if ((op == NCA_OP_LOAD_NCARR || op == NCA_OP_LOAD_SOARR) && !(((pmask | umask) >> idx) & 1u)) ok = false;
+      }
+    sp.xvec = ok ? 1 : 0;
+  }
   // as many CTAs per SM as their shared memory allows (228 KiB per SM, 1 KiB
   // reserved per CTA), at most three: ptxas caps the registers to match
   sp.minb = (int)std::max<int64_t>(1, std::min<int64_t>(3, (228 * 1024) / ((int64_t)smem + 1024)));
   sp.grp = 1;
   // tensor maps: staged operands, p operands, the stored value
-  struct Maps { CUtensorMap m[NCA_MAX_OPERANDS + 1]; };
+  struct Maps { CUtensorMap m[NCA_MAX_OPERANDS + 1 + NCA_MAX_EXTRA_OUTS]; };
   Maps maps;
   memset(&maps, 0, sizeof(maps));
   std::vector<int> other;
@@ -1394,6 +1541,7 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   for (int k = 0; k < sp.nops; ++k) if ((tmask >> k) & 1u) encode(&maps.m[mi++], s.ops[k], true);
   for (int k = 0; k < sp.nops; ++k) if ((pmask >> k) & 1u) encode(&maps.m[mi++], s.ops[k], false);
   if (sp.has_out) encode(&maps.m[mi++], s.out, false);
+  for (const CArr& a : s.xouts) encode(&maps.m[mi++], a, false);
   CUfunction fn = kernel_for(sp, tape);
   const int sms = sm_count(current_device());
   int per_sm = 0;
@@ -1668,8 +1816,9 @@ static int k4r_lastcta() {
   return (e && e[0] == '2') ? 0 : 1;
 }
 
-void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
-                 const nca_reduction* reds, int nred, cudaStream_t stream) {
+bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
+                 const nca_reduction* reds, int nred, cudaStream_t stream, const Tape* xtapes,
+                 const nca_view* xouts, int nx) {
   if (nred < 1 || nred > NCA_MAX_REDUCTIONS) fail(NCA_ERR_LIMIT, "%d reductions (1..%d)", nred, NCA_MAX_REDUCTIONS);
   if (nops < 0 || nops > NCA_MAX_OPERANDS) fail(NCA_ERR_LIMIT, "%d operands (0..%d)", nops, NCA_MAX_OPERANDS);
   if (tape.n_arrays > nops) fail(NCA_ERR_INVALID, "tape loads more operands than given");
@@ -1716,8 +1865,19 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   for (auto& r : rv) if (kept_count == 0) { r.out.ndim = 0; }
   int64_t KN = 1, RN = 1;
   for (int d = 0; d < n; ++d) { if ((mask >> d) & 1u) RN *= lshape[d]; else KN *= lshape[d]; }
-  if (KN == 0) return;
-  Space s = make_space(lshape, n, ops, nops, out, mask, rv.data(), nred);
+  if (nx > 0) {
+    // extra outputs: fused into the staged pass only (the caller runs them
+    // separately when this returns false); each has out's shape
+    if (!out || KN * RN == 0) return false;
+    for (int x = 0; x < nx; ++x) {
+      check_view(xouts[x], "extra out");
+      if (xouts[x].ndim != n) return false;
+      for (int d = 0; d < n; ++d) if (xouts[x].shape[d] != lshape[d]) return false;
+      if (xtapes[x].n_arrays > nops || xtapes[x].uses_idx) return false;
+    }
+  }
+  if (KN == 0) return true;
+  Space s = make_space(lshape, n, ops, nops, out, mask, rv.data(), nred, xouts, nx);
   const int dev = current_device();
   const int sms = sm_count(dev);
   Spec sp;
@@ -1726,9 +1886,15 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   sp.has_sum = has_sum; sp.has_max = has_max; sp.has_min = has_min;
   for (int k = 0; k < nops; ++k) sp.op_dtypes.push_back(ops[k].dtype);
   for (int k = 0; k < nops; ++k) if (s.ops[k].ptr) sp.ptrmask |= 1u << k;
+  for (int x = 0; x < nx; ++x) {
+    sp.xtapes.push_back(xtapes[x]);
+    sp.xout_dtypes.push_back(xouts[x].dtype);
+    sp.nscal += (int)xtapes[x].scalar_dtypes.size();
+  }
   merge_dims(s);
   ensure_nd1(s);
   const bool inner_reduced = (RN == 0) || s.red[s.nd - 1];
+  if (nx > 0 && (inner_reduced || sp.ptrmask != 0 || tape.uses_idx)) return false;
   if (inner_reduced && out) fail(NCA_ERR_UNSUPPORTED, "storing the expression while reducing its innermost axis is not supported; reduce without expr_out");
   if (inner_reduced) {
     // order [kept..., reduced...]
@@ -1824,7 +1990,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     std::vector<int> choice;
     if (tune_get(key, choice) && choice.size() == 1 && team_ok(choice[0])) {
       run_team(choice[0]);
-      return;
+      return true;
     }
     std::vector<nca_view> routs;
     for (int k = 0; k < nred; ++k) routs.push_back(rv[(size_t)k].out);
@@ -1836,10 +2002,10 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       const int best = tune_pick(stream, (int)cands.size(), [&](int i) { run_team(cands[(size_t)i]); });
       tune_put(key, {cands[(size_t)best]});
       run_team(cands[(size_t)best]);
-      return;
+      return true;
     }
     run_team(heur_team);
-    return;
+    return true;
   }
   // innermost dim kept. Operands strided along it but contiguous along another
   // kept dim q are staged through shared memory (kind 6); otherwise RED_OUTER.
@@ -1849,10 +2015,12 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     int nt = 0;
     const int qd = (tape.uses_idx || sp.ptrmask != 0) ? -1 : find_staged(s, tmask, nt);
     if (qd >= 0) {
+      if (nx > 0) return launch_staged_async(s, sp, tape, qd, tmask, nt, KN, RN, stream);
       launch_staged(s, sp, tape, qd, tmask, nt, KN, RN, stream);
-      return;
+      return true;
     }
   }
+  if (nx > 0) return false;
   sp.kind = 4;
   sp.kept_mask = 0;
   for (int d = 0; d < s.nd; ++d) if (!s.red[d]) sp.kept_mask |= 1u << d;
@@ -1951,7 +2119,7 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       (choice[0] == 4 || choice[0] == 8 || (rows_ok && (choice[0] == 102 || choice[0] == 104))) &&
       (choice[1] == 512 || choice[1] == 1024 || choice[1] == 2048) && (choice[2] == 0 || choice[2] == 1)) {
     run_k4(choice[0], choice[1], choice[2]);
-    return;
+    return true;
   }
   std::vector<nca_view> routs;
   for (int k = 0; k < nred; ++k) routs.push_back(rv[(size_t)k].out);
@@ -1967,10 +2135,37 @@ void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     });
     tune_put(key, cands[(size_t)best]);
     run_k4(cands[(size_t)best][0], cands[(size_t)best][1], cands[(size_t)best][2]);
-    return;
+    return true;
   }
   if (rows_ok && !k4r_off()) run_k4(104, 1024, k4r_lastcta());
   else run_k4(4, 1024, 0);
+  return true;
+}
+
+
+// tapes[0] stored to outs[0] and reduced, tapes[1..] stored to outs[1..]:
+// one staged pass when the outputs overlap neither the operands nor each
+// other and the views fit it, else the calls one after another
+void expr_multi(const std::vector<Tape>& tapes, const nca_view* ops, int nops, const nca_view* outs,
+                const nca_reduction* reds, int nred, cudaStream_t stream) {
+  const int nx = (int)tapes.size() - 1;
+  if (nx < 0) fail(NCA_ERR_INVALID, "at least one tape");
+  if (nx > NCA_MAX_EXTRA_OUTS) fail(NCA_ERR_LIMIT, "%d extra outputs (at most %d)", nx, NCA_MAX_EXTRA_OUTS);
+  bool fuse = nx > 0 && nred > 0;
+  if (fuse) {
+    std::vector<nca_view> all(outs, outs + nx + 1);
+    for (int k = 0; k < nred; ++k) all.push_back(reds[k].out);
+    fuse = rerun_safe(ops, nops, all.data(), (int)all.size());
+    for (size_t i = 0; fuse && i < all.size(); ++i)
+      for (size_t j = i + 1; fuse && j < all.size(); ++j) {
+        uintptr_t l1, h1, l2, h2;
+        if (!view_range(all[i], l1, h1) || !view_range(all[j], l2, h2) || (l1 < h2 && l2 < h1)) fuse = false;
+      }
+  }
+  if (fuse && expr_reduce(tapes[0], ops, nops, &outs[0], reds, nred, stream, tapes.data() + 1, outs + 1, nx)) return;
+  if (nred > 0) expr_reduce(tapes[0], ops, nops, &outs[0], reds, nred, stream);
+  else expr_eval(tapes[0], ops, nops, outs[0], stream);
+  for (int x = 1; x <= nx; ++x) expr_eval(tapes[(size_t)x], ops, nops, outs[x], stream);
 }
 
 }  // namespace nca
@@ -2093,6 +2288,20 @@ int jit_selftest(const char* arch) {
       ++n;
       // one output tile (three stages fit beside it)
       a7.nob = 1; a7.ns = 3;
+      nvrtc_compile(gen_source(a7, t), a);
+      ++n;
+      // an extra output: (x1 * 3 + 7) % 11 in int32 over the p-row operand
+      Tape xt;
+      xt.instrs = {I(NCA_OP_LOAD_NCARR, 1), I(NCA_OP_LOAD_CONST, 0), I(NCA_OP_MUL, 0), I(NCA_OP_LOAD_CONST, 1),
+                   I(NCA_OP_ADD, 0), I(NCA_OP_LOAD_CONST, 2), I(NCA_OP_MOD, 0)};
+      xt.scalar_dtypes = {NCA_INT32, NCA_INT32, NCA_INT32};
+      xt.scalar_slots = {3, 7, 11};
+      xt.compute_dtype = NCA_INT32; xt.result_dtype = NCA_INT32; xt.n_arrays = 2;
+      a7.nob = 2; a7.ns = 2; a7.nd = 4; a7.kept_mask = 1u | 2u | 8u; a7.ld = 2;
+      a7.xtapes = {xt}; a7.xout_dtypes = {NCA_INT32}; a7.nscal = 4; a7.nmaps = 4;
+      nvrtc_compile(gen_source(a7, t), a);
+      ++n;
+      a7.xvec = 1;   // the same on whole 16-byte tile chunks (operand 1 is a p-row operand)
       nvrtc_compile(gen_source(a7, t), a);
       ++n;
     }

@@ -28,9 +28,18 @@ Tape make_tape(const nca_tape* t, int n_operands);
 void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& out,
                cudaStream_t stream);
 
-// one pass: optional out, reductions sharing one axes mask
-void expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
-                 const nca_reduction* reds, int nred, cudaStream_t stream);
+// one pass: optional out, reductions sharing one axes mask. With nx extra
+// tapes (same operands, each stored to xouts[i] of out's shape) the call runs
+// only when all of them fuse into the one pass and returns false, launching
+// nothing, when they do not; without extras it always runs and returns true.
+bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
+                 const nca_reduction* reds, int nred, cudaStream_t stream, const Tape* xtapes = nullptr,
+                 const nca_view* xouts = nullptr, int nx = 0);
+
+// tapes[0] stored to outs[0] and reduced by reds (nred may be 0), tapes[1..]
+// stored to outs[1..]; one pass when it can (see nca_expr_multi)
+void expr_multi(const std::vector<Tape>& tapes, const nca_view* ops, int nops, const nca_view* outs,
+                const nca_reduction* reds, int nred, cudaStream_t stream);
 
 // expected output dtype of a reduction op over values of dtype `in_dt`
 int reduce_out_dtype(int op, int in_dt);
