@@ -99,8 +99,17 @@ struct NcaBPart { double s; double v; long long i; long long pad; };
 struct NcaBRes { double value; long long index; };
 struct NcaBArgs {
   const NcaBItem* items; const NcaBChunk* chunks; NcaBPart* parts; unsigned* cnt; NcaBRes* res;
-  const u64* scal; long long nchunks;
+  const u64* scal; long long nchunks; int* status;
 };
+// threads of the consumer block (the pipelined form adds a producer warp) and
+// the barrier over them
+#if NCA_BPIPE
+#define NCA_BT 256
+__device__ __forceinline__ void nca_bsync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+#else
+#define NCA_BT 256
+__device__ __forceinline__ void nca_bsync() { __syncthreads(); }
+#endif
 
 template <class R> __device__ __forceinline__ R nca_blo();
 template <> __device__ __forceinline__ float nca_blo<float>() { return __uint_as_float(0xff7fffffu); }
@@ -187,19 +196,19 @@ __device__ __forceinline__ NcaBPart nca_bshfl_merge(NcaBPart p) {
   return p;
 }
 
-// block tree of one partial per thread; valid in thread 0 (blockDim.x == 256)
+// block tree of one partial per consumer thread; valid in thread 0 (NCA_BT == 256)
 template <int K, bool IDX>
 __device__ __forceinline__ NcaBPart nca_bblock(NcaBPart p, NcaBPart* sh) {
   p = nca_bshfl_merge<K, IDX>(p);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) sh[wid] = p;
-  __syncthreads();
+  nca_bsync();
   if (wid == 0) {
     if (lane < 8) p = sh[lane];
     else { p.s = 0.0; p.v = K == 1 ? -__longlong_as_double(0x7ff0000000000000ll) : __longlong_as_double(0x7ff0000000000000ll); p.i = -1; }
     p = nca_bshfl_merge<K, IDX>(p);
   }
-  __syncthreads();
+  nca_bsync();
   return p;
 }
 
@@ -269,6 +278,77 @@ template <class T, class F> __device__ __forceinline__ void nca_bwalk_int(const 
   const T* p = (const T*)base + b;
   for (i64 i = threadIdx.x; i < n; i += blockDim.x) f.one(__ldcs(p + i), b + i);
 }
+
+#if NCA_BPIPE
+// ---- pipelined form: a producer warp streams each chunk's 16-byte aligned
+// body through NCA_BNS shared-memory slabs of NCA_BSLAB bytes by bulk copies
+// (full / empty mbarriers); the consumer threads take the unaligned head and
+// tail elements with plain loads and the body from the slabs. Every wait is
+// bounded (2 s): one that runs out records NCA_ERR_TIMEOUT in the status word,
+// stops the producer, and the consumers finish without waiting (void results).
+__device__ __forceinline__ u64 nca_bgt() { u64 t; asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t)); return t; }
+__device__ __forceinline__ bool nca_btry(u32 bar, u32 par) {
+  u32 ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+               : "=r"(ok) : "r"(bar), "r"(par) : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool nca_bwait(u32 bar, u32 par) {
+  if (nca_btry(bar, par)) return true;
+  const u64 t0 = nca_bgt();
+  while (true) {
+    if (nca_btry(bar, par)) return true;
+    if (nca_bgt() - t0 > 2000000000ull) return false;
+  }
+}
+struct NcaBPipe {
+  u32 slabs, full0, empty0;   // shared addresses
+  const unsigned char* sm;    // generic pointer of slab 0
+  long long k;                // slabs consumed by this CTA so far
+  bool dead;                  // a wait ran out: no more waits, results void
+  volatile int* stop;
+};
+// the 16-byte aligned body [a, e) of a chunk (a == e: none, every element scalar)
+__device__ __forceinline__ void nca_bbody(const NcaBItem& it, const NcaBChunk& c, unsigned long long& p0,
+                                          unsigned long long& a, unsigned long long& e) {
+  const unsigned long long es = (unsigned long long)it.pad;
+  p0 = (unsigned long long)it.data + (unsigned long long)c.begin * es;
+  const unsigned long long p1 = p0 + (unsigned long long)c.count * es;
+  a = (p0 + 15ull) & ~15ull;
+  e = p1 & ~15ull;
+  if (e <= a || (p0 % es) != 0ull) { a = p1; e = p1; }
+}
+// one chunk: head and tail elements by plain loads (LOAD(i) gives element i of
+// the chunk), the body slab by slab (VEC(v, i) takes the 16-byte vector v
+// whose first element has chunk index i)
+template <int ES, class F, class LOAD, class VEC>
+__device__ __forceinline__ void nca_bpipe_chunk(const NcaBArgs& A, const NcaBItem& it, const NcaBChunk& c, F& f,
+                                                NcaBPipe& P, LOAD ld, VEC vec) {
+  unsigned long long p0, a, e;
+  nca_bbody(it, c, p0, a, e);
+  const i64 nh = (i64)((a - p0) / ES), ne = (i64)((e - a) / ES);
+  for (i64 i = threadIdx.x; i < nh; i += NCA_BT) ld(i, c.begin + i);
+  for (i64 i = nh + ne + threadIdx.x; i < c.count; i += NCA_BT) ld(i, c.begin + i);
+  const int lane = threadIdx.x & 31;
+  for (unsigned long long src = a; src < e; src += NCA_BSLAB, ++P.k) {
+    const int k = (int)(P.k % NCA_BNS);
+    if (!P.dead && *P.stop) P.dead = true;
+    if (!P.dead && !nca_bwait(P.full0 + 8u * (u32)k, (u32)((P.k / NCA_BNS) & 1))) {
+      P.dead = true;
+      if (lane == 0) { atomicExch(A.status, 1); *P.stop = 1; }
+    }
+    if (!P.dead) {
+      const unsigned long long left = e - src;
+      const int nv = (int)((left < (unsigned long long)NCA_BSLAB ? left : (unsigned long long)NCA_BSLAB) / 16ull);
+      const uint4* v = (const uint4*)(P.sm + (size_t)k * NCA_BSLAB);
+      const i64 i0 = c.begin + nh + (i64)((src - a) / ES);
+      for (int j = threadIdx.x; j < nv; j += NCA_BT) vec(v[j], i0 + (i64)j * (16 / ES));
+    }
+    __syncwarp();
+    if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(P.empty0 + 8u * (u32)k) : "memory");
+  }
+}
+#endif
 )NCB";
 
 const char* kBatchKernel = R"NCB(
@@ -296,6 +376,78 @@ extern "C" __global__ void __launch_bounds__(256) nca_batch_expr(const NcaBArgs 
 }
 )NCB";
 
+const char* kBatchKernelPipe = R"NCB(
+extern "C" __global__ void __launch_bounds__(288) nca_batch_expr(const NcaBArgs A) {
+  extern __shared__ __align__(128) unsigned char nca_bsm[];
+  __shared__ NcaBPart sh[8];
+  __shared__ int last;
+  __shared__ volatile int stop;
+  const u32 sbase = (u32)__cvta_generic_to_shared(nca_bsm);
+  const u32 full0 = sbase + NCA_BNS * NCA_BSLAB, empty0 = full0 + 8 * NCA_BNS;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) {
+    stop = 0;
+    for (int k = 0; k < NCA_BNS; ++k) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8 * k) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(empty0 + 8 * k) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (wid == 8) {
+    // producer: lane 0 copies the bodies of this CTA's chunks slab by slab
+    if (lane != 0) return;
+    long long issued = 0;
+    bool bad = false;
+    for (long long cid = blockIdx.x; cid < A.nchunks && !bad; cid += gridDim.x) {
+      const NcaBChunk c = A.chunks[cid];
+      const NcaBItem it = A.items[c.item];
+      unsigned long long p0, a, e;
+      nca_bbody(it, c, p0, a, e);
+      for (unsigned long long src = a; src < e; src += NCA_BSLAB, ++issued) {
+        const int k = (int)(issued % NCA_BNS);
+        if (issued >= NCA_BNS && !nca_bwait(empty0 + 8 * k, (u32)((issued / NCA_BNS - 1) & 1))) { bad = true; break; }
+        if (stop) { bad = true; break; }
+        const unsigned long long left = e - src;
+        const u32 bytes = (u32)(left < (unsigned long long)NCA_BSLAB ? left : (unsigned long long)NCA_BSLAB);
+        const u32 bar = full0 + 8 * k;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(sbase + (u32)(k * NCA_BSLAB)), "l"(src), "r"(bytes), "r"(bar) : "memory");
+      }
+    }
+    if (bad) {
+      atomicExch(A.status, 1);
+      stop = 1;
+      // the copies still in flight land before the CTA's shared memory goes away
+      for (long long j = issued > NCA_BNS ? issued - NCA_BNS : 0; j < issued; ++j)
+        nca_bwait(full0 + 8 * (int)(j % NCA_BNS), (u32)((j / NCA_BNS) & 1));
+    }
+    return;
+  }
+  NcaBPipe P;
+  P.slabs = sbase; P.full0 = full0; P.empty0 = empty0; P.sm = nca_bsm; P.k = 0; P.dead = false; P.stop = &stop;
+  for (long long cid = blockIdx.x; cid < A.nchunks; cid += gridDim.x) {
+    const NcaBChunk c = A.chunks[cid];
+    const NcaBItem it = A.items[c.item];
+    nca_bdispatch(A, it, c, cid, sh, P);
+    if (it.nchunks == 1) continue;
+    // the CTA that stores the item's last partial merges them in chunk order
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last = atomicAdd(A.cnt + c.item, 1u) + 1u == (unsigned)it.nchunks;
+    }
+    nca_bsync();
+    if (last) {
+      __threadfence();
+      nca_bfinish(A, it, c.item, sh);
+      if (threadIdx.x == 0) A.cnt[c.item] = 0u;
+    }
+    nca_bsync();
+  }
+}
+)NCB";
+
 std::string dtype_walker(int dt) {
   switch (dt) {
     case NCA_FLOAT32: return "nca_bwalk_f32";
@@ -306,6 +458,45 @@ std::string dtype_walker(int dt) {
     case NCA_INT64: return "nca_bwalk_int<i64>";
   }
   nca::fail(NCA_ERR_DTYPE, "batched input dtype %d: float32, float64, bfloat16, float16, int32 or int64", dt);
+}
+
+int dtinfo_size(int dt) { return nca::dtinfo(dt).size; }
+
+// element gi of the item in the pipelined walker (plain load), as the program's load type
+std::string pipe_load(int dt, const std::string& gi) {
+  switch (dt) {
+    case NCA_FLOAT32: return "__ldcs((const float*)it.data + " + gi + ")";
+    case NCA_BFLOAT16: return "nca_bf16_to_f32(__ldcs((const unsigned short*)it.data + " + gi + "))";
+    case NCA_FLOAT16: return "nca_f16_to_f32(__ldcs((const unsigned short*)it.data + " + gi + "))";
+    case NCA_FLOAT64: return "__ldcs((const double*)it.data + " + gi + ")";
+    case NCA_INT32: return "__ldcs((const int*)it.data + " + gi + ")";
+    default: return "__ldcs((const i64*)it.data + " + gi + ")";
+  }
+}
+
+// the elements of one 16-byte vector v whose first element is gi
+std::string pipe_vec(int dt) {
+  switch (dt) {
+    case NCA_FLOAT32:
+      return "      f.two(__uint_as_float(v.x), __uint_as_float(v.y), gi);\n"
+             "      f.two(__uint_as_float(v.z), __uint_as_float(v.w), gi + 2);\n";
+    case NCA_BFLOAT16: case NCA_FLOAT16: {
+      const std::string cv = dt == NCA_FLOAT16 ? "nca_f16_to_f32" : "nca_bf16_to_f32";
+      std::string r;
+      const char* w[4] = {"v.x", "v.y", "v.z", "v.w"};
+      for (int j = 0; j < 4; ++j)
+        r += std::string("      f.two(") + cv + "((unsigned short)(" + w[j] + " & 0xffffu)), " + cv + "((unsigned short)(" +
+             w[j] + " >> 16)), gi + " + std::to_string(2 * j) + ");\n";
+      return r;
+    }
+    case NCA_FLOAT64:
+      return "      f.two(__longlong_as_double((i64)(((u64)v.y << 32) | v.x)), "
+             "__longlong_as_double((i64)(((u64)v.w << 32) | v.z)), gi);\n";
+    case NCA_INT32:
+      return "      f.two((int)v.x, (int)v.y, gi);\n      f.two((int)v.z, (int)v.w, gi + 2);\n";
+    default:
+      return "      f.two((i64)(((u64)v.y << 32) | v.x), (i64)(((u64)v.w << 32) | v.z), gi);\n";
+  }
 }
 
 const char* load_type(int dt) {
@@ -342,6 +533,8 @@ struct nca_batch_expr {
   long long chunk_bytes = 512 * 1024;   // fastest with 4 loads in flight and 4 CTAs per SM on 20,000 uneven arrays
   int unroll = 4;          // 16-byte loads per thread issued together in the walkers
   int ctas_per_sm = 4;
+  bool pipe = true;        // a producer warp streams the chunks through shared-memory slabs
+  int nslab = 4, slab = 16384;
   int ctas = 0;
   cudaGraphExec_t graph = nullptr;
   void* graph_results = nullptr;
@@ -377,7 +570,8 @@ std::vector<Acc> prog_accs(const Program& p, int* acc_of_out) {
 
 std::string gen_batch_source(const nca_batch_expr& b) {
   std::ostringstream os;
-  os << nca::jit_prelude() << "#define NCA_BUNROLL " << b.unroll << "\n" << kBatchCommon;
+  os << nca::jit_prelude() << "#define NCA_BUNROLL " << b.unroll << "\n#define NCA_BPIPE " << (b.pipe ? 1 : 0)
+     << "\n#define NCA_BNS " << b.nslab << "\n#define NCA_BSLAB " << b.slab << "\n" << kBatchCommon;
   for (size_t k = 0; k < b.tapes.size(); ++k) os << tape_fn(b.tapes[k], (int)k);
   for (size_t p = 0; p < b.progs.size(); ++p) {
     const Program& pg = b.progs[p];
@@ -409,10 +603,19 @@ std::string gen_batch_source(const nca_batch_expr& b) {
     for (size_t a = 0; a < accs.size(); ++a) os << "    a" << a << ".see2(r" << accs[a].tape << ", q" << accs[a].tape << ", i);\n";
     os << "  }\n};\n";
     // chunk of an item of program p: walk, block trees, partials or final values
-    os << "__device__ __forceinline__ void nca_bprog" << p
-       << "(const NcaBArgs& A, const NcaBItem& it, const NcaBChunk& c, long long cid, NcaBPart* sh) {\n"
-       << "  NcaBF" << p << " f; f.init(A.scal);\n"
-       << "  " << dtype_walker(pg.dtype) << "(it.data, c.begin, c.count, f);\n";
+    if (b.pipe) {
+      os << "__device__ __forceinline__ void nca_bprog" << p
+         << "(const NcaBArgs& A, const NcaBItem& it, const NcaBChunk& c, long long cid, NcaBPart* sh, NcaBPipe& P) {\n"
+         << "  NcaBF" << p << " f; f.init(A.scal);\n"
+         << "  nca_bpipe_chunk<" << dtinfo_size(pg.dtype) << ">(A, it, c, f, P,\n"
+         << "    [&](i64 i, i64 gi) { (void)i; f.one(" << pipe_load(pg.dtype, "gi") << ", gi); },\n"
+         << "    [&](const uint4 v, i64 gi) {\n" << pipe_vec(pg.dtype) << "    });\n";
+    } else {
+      os << "__device__ __forceinline__ void nca_bprog" << p
+         << "(const NcaBArgs& A, const NcaBItem& it, const NcaBChunk& c, long long cid, NcaBPart* sh) {\n"
+         << "  NcaBF" << p << " f; f.init(A.scal);\n"
+         << "  " << dtype_walker(pg.dtype) << "(it.data, c.begin, c.count, f);\n";
+    }
     for (size_t a = 0; a < accs.size(); ++a) {
       os << "  {\n    const NcaBPart m = nca_bblock<" << accs[a].kind << ", " << (accs[a].idx ? "true" : "false")
          << ">(f.a" << a << ".part(), sh);\n    if (threadIdx.x == 0) {\n";
@@ -437,7 +640,7 @@ std::string gen_batch_source(const nca_batch_expr& b) {
       const std::string R = nca::jit_ctype(b.tapes[(size_t)accs[a].tape].result_dtype);
       os << "  {\n    NcaBPart m; m.s = 0.0; m.i = -1; m.pad = 0;\n"
          << "    m.v = (double)" << (K == 1 ? "nca_blo<" : "nca_bhi<") << R << ">();\n"
-         << "    for (int k = threadIdx.x; k < it.nchunks; k += blockDim.x) {\n"
+         << "    for (int k = threadIdx.x; k < it.nchunks; k += NCA_BT) {\n"
          << "      NcaBPart o = A.parts[(long long)(it.first_chunk + k) * " << NCA_BATCH_MAX_OUTS << " + " << a << "];\n"
          << "      nca_bmerge<" << K << ", " << IDX << ">(m, o);\n    }\n"
          << "    m = nca_bblock<" << K << ", " << IDX << ">(m, sh);\n    if (threadIdx.x == 0) {\n";
@@ -452,11 +655,14 @@ std::string gen_batch_source(const nca_batch_expr& b) {
     }
     os << "}\n";
   }
-  os << "__device__ __forceinline__ void nca_bdispatch(const NcaBArgs& A, const NcaBItem& it, const NcaBChunk& c, long long cid, NcaBPart* sh) {\n  switch (it.prog) {\n";
-  for (size_t p = 0; p < b.progs.size(); ++p) os << "    case " << p << ": nca_bprog" << p << "(A, it, c, cid, sh); break;\n";
+  const std::string PX = b.pipe ? ", NcaBPipe& P" : "";
+  const std::string PA = b.pipe ? ", P" : "";
+  os << "__device__ __forceinline__ void nca_bdispatch(const NcaBArgs& A, const NcaBItem& it, const NcaBChunk& c, long long cid, NcaBPart* sh"
+     << PX << ") {\n  switch (it.prog) {\n";
+  for (size_t p = 0; p < b.progs.size(); ++p) os << "    case " << p << ": nca_bprog" << p << "(A, it, c, cid, sh" << PA << "); break;\n";
   os << "  }\n}\n__device__ __forceinline__ void nca_bfinish(const NcaBArgs& A, const NcaBItem& it, int item, NcaBPart* sh) {\n  switch (it.prog) {\n";
   for (size_t p = 0; p < b.progs.size(); ++p) os << "    case " << p << ": nca_bfin" << p << "(A, it, item, sh); break;\n";
-  os << "  }\n}\n" << kBatchKernel;
+  os << "  }\n}\n" << (b.pipe ? kBatchKernelPipe : kBatchKernel);
   return os.str();
 }
 
@@ -468,15 +674,20 @@ struct Args {
   void* res;
   const void* scal;
   long long nchunks;
+  int* status;
 };
+
+// dynamic shared memory of the pipelined form: the slabs and two mbarriers per slab
+size_t pipe_smem(const nca_batch_expr& b) { return b.pipe ? (size_t)b.nslab * (size_t)b.slab + 16 * (size_t)b.nslab : 0; }
 
 void launch(nca_batch_expr* b, void* results, cudaStream_t s) {
   if (b->nchunks == 0) return;
-  Args a{b->d_items, b->d_chunks, b->d_parts, b->d_cnt, results, b->d_scal, b->nchunks};
+  Args a{b->d_items, b->d_chunks, b->d_parts, b->d_cnt, results, b->d_scal, b->nchunks, nca::jit_status_word()};
   void* params[] = {&a};
   nca::count_launch();
-  nca::check_cu(nca::drv().cuLaunchKernel(b->fn, (unsigned)std::min<long long>(b->ctas, b->nchunks), 1, 1, 256, 1, 1,
-                                          0, (CUstream)s, params, nullptr),
+  nca::check_cu(nca::drv().cuLaunchKernel(b->fn, (unsigned)std::min<long long>(b->ctas, b->nchunks), 1, 1,
+                                          b->pipe ? 288 : 256, 1, 1, (unsigned)pipe_smem(*b), (CUstream)s, params,
+                                          nullptr),
                 "cuLaunchKernel(batched expressions)");
 }
 
@@ -522,6 +733,10 @@ extern "C" int32_t nca_batch_expr_create(const nca_batch_expr_item* items, int32
     if (const char* e = getenv("NCA_BATCH_EXPR_CHUNK")) b->chunk_bytes = std::max(4096ll, atoll(e));
     if (const char* e = getenv("NCA_BATCH_EXPR_UNROLL")) b->unroll = std::max(1, std::min(16, atoi(e)));
     if (const char* e = getenv("NCA_BATCH_EXPR_CTAS")) b->ctas_per_sm = std::max(1, std::min(8, atoi(e)));
+    if (const char* e = getenv("NCA_BATCH_EXPR_PIPE")) b->pipe = e[0] != '0';
+    if (const char* e = getenv("NCA_BATCH_EXPR_SLAB")) b->slab = std::max(1024, std::min(65536, atoi(e) / 16 * 16));
+    if (const char* e = getenv("NCA_BATCH_EXPR_NSLAB")) b->nslab = std::max(2, std::min(8, atoi(e)));
+    if (b->pipe && !getenv("NCA_BATCH_EXPR_CTAS")) b->ctas_per_sm = 3;
     for (int i = 0; i < n_items; ++i) {
       const nca_batch_expr_item& it = items[i];
       if (it.length < 0) fail(NCA_ERR_SHAPE, "item %d: negative length", i);
@@ -551,7 +766,7 @@ extern "C" int32_t nca_batch_expr_create(const nca_batch_expr_item* items, int32
       const long long isz = dtinfo(it.dtype).size;
       const long long per = std::max(256ll, b->chunk_bytes / isz);
       const long long nc = it.length == 0 ? 1 : (it.length + per - 1) / per;
-      hi[(size_t)i] = ItemDev{it.data, it.length, pid, (int)hc.size(), (int)nc, 0};
+      hi[(size_t)i] = ItemDev{it.data, it.length, pid, (int)hc.size(), (int)nc, (int)isz};
       for (long long c = 0; c < nc; ++c) {
         const long long beg = c * per;
         hc.push_back(ChunkDev{i, 0, beg, std::min(per, it.length - beg)});
@@ -573,7 +788,11 @@ extern "C" int32_t nca_batch_expr_create(const nca_batch_expr_item* items, int32
     check_cuda(cudaMemsetAsync(b->d_cnt, 0, std::max<size_t>((size_t)n_items * 4, 16), s), "batch counters");
     b->fn = jit_get(gen_batch_source(*b), "nca_batch_expr");
     int per_sm = 0;
-    check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->fn, 256, 0), "occupancy");
+    if (b->pipe)
+      check_cu(drv().cuFuncSetAttribute(b->fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)pipe_smem(*b)),
+               "smem attribute");
+    check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b->fn, b->pipe ? 288 : 256, pipe_smem(*b)),
+             "occupancy");
     b->ctas = sm_count(b->dev) * std::max(1, std::min(per_sm, b->ctas_per_sm));
     check_cuda(cudaStreamSynchronize(s), "batch table upload");
     *out = b;
@@ -725,7 +944,15 @@ int batch_expr_selftest(const char* arch) {
   p4.dtype = NCA_INT32; p4.n_outs = 2;
   p4.tape[0] = 3; p4.op[0] = NCA_RED_ARGMAX; p4.tape[1] = 0; p4.op[1] = NCA_RED_MEAN;
   b.progs = {p1, p2, p3, p4};
+  b.pipe = false;
   jit_compile_only(gen_batch_source(b), arch);
-  return 1;
+  b.pipe = true;   // the pipelined form (producer warp, shared-memory slabs)
+  Program p5 = p4;
+  p5.dtype = NCA_INT64;
+  Program p6 = p2;
+  p6.dtype = NCA_FLOAT16;
+  b.progs = {p1, p2, p3, p4, p5, p6};
+  jit_compile_only(gen_batch_source(b), arch);
+  return 2;
 }
 }  // namespace nca

@@ -24,6 +24,10 @@ struct Tape {
 
 Tape make_tape(const nca_tape* t, int n_operands);
 
+// The device int that kernels with bounded waits set when a wait gives up
+// (read and cleared by nca_device_status).
+int* jit_status_word();
+
 // out = tape(operands)
 void expr_eval(const Tape& tape, const nca_view* ops, int nops, const nca_view& out,
                cudaStream_t stream);

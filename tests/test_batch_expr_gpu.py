@@ -181,3 +181,45 @@ def test_special_values(cuda, orc):
                 assert vals[i, o] == float(orc.reduce(h, 10, 2))
             else:
                 assert idxs[i, o] == int(orc.reduce(h, 10, int(op))), (i, op)
+
+
+def test_pipelined_and_direct_forms_agree(cuda, orc):
+    """The pipelined form (producer warp, shared-memory slabs: the default) and
+    the direct-load form (NCA_BATCH_EXPR_PIPE=0) on arrays whose starts are not
+    16-byte aligned, shorter than one vector, and spanning many slabs and
+    chunks: extremes and indices equal, sums within the stated bound of the
+    oracle."""
+    import os
+    rng = np.random.default_rng(SEED + 603)
+    lens = [1, 3, 5, 17, 4095, 4097, 65539, 1 << 20, (1 << 21) + 7]
+    items_h, items, spec = [], [], []
+    for i, n in enumerate(lens):
+        for dt in (DType.float32, DType.bfloat16, DType.float64, DType.int32):
+            h = _host(rng, dt, n + 3)
+            d = nca.NCDevArray.from_host(h, dt)
+            off = i % 4          # 0..3 elements in: every start alignment
+            d, h = d[off:off + n], h[off:off + n]
+            pool = INT_PATTERNS if dt == DType.int32 else FLOAT_PATTERNS
+            outs = pool[i % len(pool)]
+            items.append((d, [(FNS[f], op) for f, op in outs]))
+            items_h.append((h, dt))
+            spec.append(outs)
+    res = {}
+    for mode in ("1", "0"):
+        old = os.environ.get("NCA_BATCH_EXPR_PIPE")
+        os.environ["NCA_BATCH_EXPR_PIPE"] = mode
+        try:
+            b = _build(items)
+            res[mode] = b.run(graph=(mode == "1")) + (b,)
+        finally:
+            if old is None:
+                del os.environ["NCA_BATCH_EXPR_PIPE"]
+            else:
+                os.environ["NCA_BATCH_EXPR_PIPE"] = old
+    v1, i1, b1 = res["1"]
+    v0, i0, b0 = res["0"]
+    bad = [(k, o, int(i1[k, o]), int(i0[k, o]), items[k][0].size, int(items_h[k][1]), spec[k][o])
+           for k in range(len(items)) for o in range(len(spec[k])) if i1[k, o] != i0[k, o]]
+    assert not bad, bad[:8]
+    _check(orc, b1, items_h, spec, v1, i1)
+    _check(orc, b0, items_h, spec, v0, i0)
