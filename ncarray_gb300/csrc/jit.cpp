@@ -363,6 +363,7 @@ struct Spec {
   int block = 256;   // kinds 1, 2: threads per block (NCA_LB)
   int k4r = 0;       // kind 4: row lanes per warp (row-lane form, one reduced dim rd); 0: thread per column group
   int rd = 0;
+  int k4p = 0;       // kind 4 row-lane form on a persistent grid (equal contiguous ranges of units)
   // kind 7: extra outputs, each a tape over the same operands stored elementwise
   std::vector<Tape> xtapes;
   std::vector<int> xout_dtypes;
@@ -619,7 +620,7 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_HAS_OUT " << (sp.has_out ? 1 : 0) << "\n#define NCA_NWORDS " << L.nwords
      << "\n#define NCA_HAS_SUM " << (sp.has_sum ? 1 : 0) << "\n#define NCA_HAS_MAX " << (sp.has_max ? 1 : 0)
      << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n#define NCA_LASTCTA " << sp.lastcta
-     << "\n#define NCA_K4R " << sp.k4r << "\n#define NCA_RD " << sp.rd << "\n";
+     << "\n#define NCA_K4R " << sp.k4r << "\n#define NCA_RD " << sp.rd << "\n#define NCA_K4P " << sp.k4p << "\n";
   int sum_mode = 1;
   if (sp.nred > 0) {
     const int ra = arith_dtype(sp.r);
@@ -1089,7 +1090,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.has_sum); add(sp.has_max); add(sp.has_min); add(sp.nscal); add(sp.qd); add(sp.qx); add(sp.tp);
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
   add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
-  add(sp.nob); add(sp.lastcta); add(sp.block); add(sp.k4r); add(sp.rd);
+  add(sp.nob); add(sp.lastcta); add(sp.block); add(sp.k4r); add(sp.rd); add(sp.k4p);
   k += literal_key(t) + '|';
   add(sp.xvec);
   for (size_t x = 0; x < sp.xtapes.size(); ++x) {
@@ -1815,6 +1816,13 @@ static int k4r_lastcta() {
   const char* e = getenv("NCA_K4_ROWS");
   return (e && e[0] == '2') ? 0 : 1;
 }
+// NCA_K4_ROWS=3: the row-lane form on a persistent grid of equal unit ranges
+// (a tuner candidate; measured slower than the splits on (4096, 16384) axis 0,
+// 0.66 against 0.73, and (256, 256, 1024) axis 1, 0.74 against 0.77)
+static bool k4r_persistent() {
+  const char* e = getenv("NCA_K4_ROWS");
+  return e && e[0] == '3';
+}
 
 bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view* out,
                  const nca_reduction* reds, int nred, cudaStream_t stream, const Tape* xtapes,
@@ -2040,6 +2048,35 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     sp.k4r = R;
     sp.rd = rdim;
     const int64_t nset = cdiv(KG, GPC);
+    if (tps == 0) {
+      // persistent grid: every resident CTA, units of 4R rows split evenly
+      sp.k4p = 1;
+      sp.lastcta = 0;
+      CUfunction fn = kernel_for(sp, tape);
+      int per_sm = 0;
+      check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0), "occupancy");
+      const int64_t W = nset * cdiv(RN, 4 * R);
+      const int64_t G = std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * std::max(per_sm, 1), W));
+      const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
+      std::vector<uint64_t> w;
+      fill_common_words(s, sp, tape, L, w);
+      w[L.nsplit] = (uint64_t)G; w[L.chunk] = 0; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+      const int64_t slots = (G + nset) * GPC * sp.vec;
+      const size_t pbytes = (size_t)slots * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0));
+      const size_t cbytes = ((size_t)nset * 4 + 255) / 256 * 256;
+      StreamScratch part(pbytes + cbytes, stream);
+      uint64_t* p = (uint64_t*)part.ptr;
+      if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += slots; }
+      if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * slots; }
+      if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * slots; }
+      w[L.aux] = (uint64_t)(uintptr_t)p;
+      check_cuda(cudaMemsetAsync(p, 0, cbytes, stream), "arrival counters");
+      launch(fn, G, w, stream);
+      sp.k4r = 0;
+      sp.rd = 0;
+      sp.k4p = 0;
+      return;
+    }
     const int64_t target = (int64_t)sms * tps;
     int64_t S = std::max<int64_t>(1, std::min<int64_t>(cdiv(target, nset * 256), RN / (8 * R)));
     int64_t C = cdiv(RN, S);
@@ -2117,7 +2154,8 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
   std::vector<int> choice;
   if (tune_get(key, choice) && choice.size() == 3 &&
       (choice[0] == 4 || choice[0] == 8 || (rows_ok && (choice[0] == 102 || choice[0] == 104))) &&
-      (choice[1] == 512 || choice[1] == 1024 || choice[1] == 2048) && (choice[2] == 0 || choice[2] == 1)) {
+      (choice[1] == 512 || choice[1] == 1024 || choice[1] == 2048 || (choice[0] >= 100 && choice[1] == 0)) &&
+      (choice[2] == 0 || choice[2] == 1)) {
     run_k4(choice[0], choice[1], choice[2]);
     return true;
   }
@@ -2128,7 +2166,7 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     std::vector<std::vector<int>> cands = {{4, 1024, 0}, {8, 1024, 0}, {4, 2048, 0}, {8, 2048, 0}, {8, 512, 0},
                                            {4, 1024, 1}, {8, 512, 1}};
     if (rows_ok)
-      for (auto c : std::vector<std::vector<int>>{{104, 2048, 1}, {104, 2048, 0}, {102, 2048, 1}, {104, 1024, 1}})
+      for (auto c : std::vector<std::vector<int>>{{104, 0, 0}, {104, 2048, 1}, {104, 2048, 0}, {102, 2048, 1}, {104, 1024, 1}})
         cands.push_back(c);
     const int best = tune_pick(stream, (int)cands.size(), [&](int i) {
       run_k4(cands[(size_t)i][0], cands[(size_t)i][1], cands[(size_t)i][2]);
@@ -2137,7 +2175,7 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     run_k4(cands[(size_t)best][0], cands[(size_t)best][1], cands[(size_t)best][2]);
     return true;
   }
-  if (rows_ok && !k4r_off()) run_k4(104, 1024, k4r_lastcta());
+  if (rows_ok && !k4r_off()) run_k4(104, k4r_persistent() ? 0 : 1024, k4r_lastcta());
   else run_k4(4, 1024, 0);
   return true;
 }
@@ -2232,6 +2270,9 @@ int jit_selftest(const char* arch) {
       if (kind == 4) {                 // row-lane form over the one reduced dim 1
         Spec s4 = sp;
         s4.k4r = 4; s4.rd = 1; s4.lastcta = 1; s4.unroll = 4;
+        nvrtc_compile(gen_source(s4, t), a);
+        ++n;
+        s4.lastcta = 0; s4.k4p = 1;    // on a persistent grid
         nvrtc_compile(gen_source(s4, t), a);
         ++n;
       }

@@ -1,7 +1,7 @@
-"""Outer reductions (innermost axis kept) in their three schedules against the
-oracle: the row-lane form with the last CTA merging the splits (default),
-the row-lane form with a finalize launch (NCA_K4_ROWS=2) and the
-thread-per-column-group form (NCA_K4_ROWS=0). Max/min/argmax/argmin and
+"""Outer reductions (innermost axis kept) in their four schedules against the
+oracle: the row-lane form on splits with the last CTA merging them (default),
+with a finalize launch (NCA_K4_ROWS=2) or on a persistent grid of equal unit
+ranges (NCA_K4_ROWS=3), and the thread-per-column-group form (NCA_K4_ROWS=0). Max/min/argmax/argmin and
 integer sums bit-exact, float sums within the tolerances of
 test_reduce_gpu; the stored expression value bit-exact.
 
@@ -21,17 +21,20 @@ from tests.test_reduce_gpu import check_reduction
 
 pytestmark = pytest.mark.gpu
 
-MODES = ["1", "2", "0"]
+MODES = ["default", "3", "2", "0"]
 
 
 def _with_mode(mode, fn):
     old = os.environ.get("NCA_K4_ROWS")
-    os.environ["NCA_K4_ROWS"] = mode
+    if mode == "default":
+        os.environ.pop("NCA_K4_ROWS", None)
+    else:
+        os.environ["NCA_K4_ROWS"] = mode
     try:
         return fn()
     finally:
         if old is None:
-            del os.environ["NCA_K4_ROWS"]
+            os.environ.pop("NCA_K4_ROWS", None)
         else:
             os.environ["NCA_K4_ROWS"] = old
 
