@@ -1452,12 +1452,15 @@ static bool launch_staged_async(const Space& s, Spec sp, const Tape& tape, int q
   // CTAs per SM)
   // with extra outputs (one more output tile each) the block shrinks so that
   // two CTAs still fit on an SM: (8, 256, 256, 64) with one extra output ran
-  // 4.96 TB/s at 64 rows, 3.66 TB/s at 128 rows (one CTA per SM)
+  // 4.96 TB/s at 64 rows, 3.66 TB/s at 128 rows (one CTA per SM), before the
+  // extra tape ran on whole tile chunks
   const int64_t budget = sp.xtapes.empty() ? 227 * 1024 : 113 * 1024;
   const int tp = 32;
   int rb_max = (int)std::max<int64_t>(1, 128 / QX);
   if (const char* e = getenv("NCA_STAGED_RB")) { const int v = atoi(e); if (v >= 1 && v <= 16) rb_max = v; }
-  int ns_want = 2;
+  // 2 stages; 3 with extra outputs (the one-pass C2 step: 64 rows, 3 stages,
+  // 2 CTAs per SM 5.68 TB/s against 5.51 for 2 stages and 3 CTAs per SM)
+  int ns_want = sp.xtapes.empty() ? 2 : 3;
   if (const char* e = getenv("NCA_STAGED_STAGES")) { const int v = atoi(e); if (v >= 2 && v <= 6) ns_want = v; }
   int nob = 2;
   if (const char* e = getenv("NCA_STAGED_OUTBUFS")) { const int v = atoi(e); if (v == 1 || v == 2) nob = v; }
