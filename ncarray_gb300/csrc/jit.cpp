@@ -2184,8 +2184,10 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
     return true;
   }
   // row-lane form: 8 rows in flight per row lane (the tuner's choice on the
-  // outer-axis benchmarks and C1: max over axis 1 0.77 -> 0.81 of measured)
-  if (rows_ok && !k4r_off()) run_k4(108, k4r_persistent() ? 0 : 1024, k4r_lastcta());
+  // outer-axis benchmarks and C1: max over axis 1 0.77 -> 0.81 of measured);
+  // splits for 1024 threads per SM, 512 for short reduced axes (the tuner's
+  // choices: (4096, 16384) over axis 0 and C1's 128 rows)
+  if (rows_ok && !k4r_off()) run_k4(108, k4r_persistent() ? 0 : (RN <= 256 ? 512 : 1024), k4r_lastcta());
   else run_k4(4, 1024, 0);
   return true;
 }
