@@ -763,6 +763,16 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
             for e, o in zip(parts, outs):
                 for r in reds:
                     e.evaluate(out=o, reductions=r)
+    elif op == "red-global-sum-noalloc":
+        # the global sum of 64 Mi float32 (256 MB) through nca_reduce_noalloc
+        import ctypes
+        from ncarray_gb300 import _lib
+        x = torch.randn(64 << 20, device="cuda", dtype=torch.float32)
+        res = torch.zeros(1, dtype=torch.float32, device="cuda")
+        src = _lib.make_view(x.data_ptr(), int(nca.DType.float32), (64 << 20,), (4,))
+        dst = _lib.make_view(res.data_ptr(), int(nca.DType.float32), (), ())
+        fn = lambda: _lib.call("nca_reduce_noalloc", ctypes.byref(src), 0, ctypes.byref(dst),  # noqa: E731
+                               torch.cuda.current_stream().cuda_stream)
     elif op == "c5-general-small":
         # the general batched form (any tapes and reductions) on 1,000 of the uneven arrays
         from ncarray_gb300.batch import BatchExpr
