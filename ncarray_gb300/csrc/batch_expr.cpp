@@ -111,6 +111,20 @@ __device__ __forceinline__ void nca_bsync() { asm volatile("bar.sync 1, 256;" ::
 __device__ __forceinline__ void nca_bsync() { __syncthreads(); }
 #endif
 
+// a partial of a float32 result inside a block: float-float sum (h, l),
+// extreme v and its index i
+struct NcaBPartF { float h, l, v; long long i; };
+// (h, l) += (h2, l2) in float32 (TwoSum of the high parts); an infinite or
+// NaN sum keeps no error term
+__device__ __forceinline__ void nca_ffadd(float& h, float& l, float h2, float l2) {
+  const float s = __fadd_rn(h, h2);
+  if (!(fabsf(s) < __int_as_float(0x7f800000))) { h = s; l = 0.f; return; }
+  const float bb = __fsub_rn(s, h);
+  const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+  h = s;
+  l = __fadd_rn(__fadd_rn(l, l2), e);
+}
+
 template <class R> __device__ __forceinline__ R nca_blo();
 template <> __device__ __forceinline__ float nca_blo<float>() { return __uint_as_float(0xff7fffffu); }
 template <> __device__ __forceinline__ double nca_blo<double>() { return __longlong_as_double((i64)0xffefffffffffffffull); }
@@ -154,7 +168,16 @@ template <bool IDX> struct NcaBAcc<float, 0, IDX> {
     p.s = x + y; p.v = 0.0; p.i = -1; p.pad = 0;
     return p;
   }
+  __device__ __forceinline__ NcaBPartF partf() const;
 };
+template <bool IDX> __device__ __forceinline__ NcaBPartF NcaBAcc<float, 0, IDX>::partf() const {
+  NcaBPartF p;
+  p.h = hi.x;
+  p.l = nca_isfinite(hi.x) ? lo.x : 0.f;
+  nca_ffadd(p.h, p.l, hi.y, nca_isfinite(hi.y) ? lo.y : 0.f);
+  p.v = 0.f; p.i = -1;
+  return p;
+}
 template <bool IDX> struct NcaBAcc<double, 0, IDX> {
   double d;
   __device__ __forceinline__ void init() { d = 0.0; }
@@ -164,6 +187,7 @@ template <bool IDX> struct NcaBAcc<double, 0, IDX> {
 };
 template <class R, int K, bool IDX> struct NcaBAcc {
   R v; i64 i;
+  __device__ __forceinline__ NcaBPartF partf() const { NcaBPartF p; p.h = 0.f; p.l = 0.f; p.v = (float)v; p.i = i; return p; }
   __device__ __forceinline__ void init() { v = K == 1 ? nca_blo<R>() : nca_bhi<R>(); i = -1; }
   __device__ __forceinline__ void see(R a, i64 idx) {
     const bool better = K == 1 ? a > v : a < v;
@@ -210,6 +234,47 @@ __device__ __forceinline__ NcaBPart nca_bblock(NcaBPart p, NcaBPart* sh) {
   }
   nca_bsync();
   return p;
+}
+
+// the same in float32 for float32 results; thread 0 widens the result once
+template <int K, bool IDX>
+__device__ __forceinline__ void nca_bmergef(NcaBPartF& a, const NcaBPartF& b) {
+  if (K == 0) { nca_ffadd(a.h, a.l, b.h, b.l); return; }
+  const bool better = K == 1 ? b.v > a.v : b.v < a.v;
+  if (!IDX) { a.v = better ? b.v : a.v; return; }
+  if (b.i < 0) return;
+  if (a.i < 0 || better || (b.v == a.v && b.i < a.i)) { a.v = b.v; a.i = b.i; }
+}
+template <int K, bool IDX>
+__device__ __forceinline__ NcaBPartF nca_bshflf(NcaBPartF p) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    NcaBPartF o;
+    o.h = __shfl_down_sync(0xffffffffu, p.h, off);
+    o.l = __shfl_down_sync(0xffffffffu, p.l, off);
+    o.v = __shfl_down_sync(0xffffffffu, p.v, off);
+    o.i = __shfl_down_sync(0xffffffffu, p.i, off);
+    nca_bmergef<K, IDX>(p, o);
+  }
+  return p;
+}
+template <int K, bool IDX>
+__device__ __forceinline__ NcaBPart nca_bblockf(NcaBPartF p, NcaBPart* shd) {
+  NcaBPartF* sh = reinterpret_cast<NcaBPartF*>(shd);
+  p = nca_bshflf<K, IDX>(p);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = p;
+  nca_bsync();
+  if (wid == 0) {
+    if (lane < 8) p = sh[lane];
+    else { p.h = 0.f; p.l = 0.f; p.v = K == 1 ? -__int_as_float(0x7f800000) : __int_as_float(0x7f800000); p.i = -1; }
+    p = nca_bshflf<K, IDX>(p);
+  }
+  nca_bsync();
+  NcaBPart r;
+  r.s = nca_isfinite(p.h) ? (double)p.h + (double)p.l : (double)p.h;
+  r.v = (double)p.v; r.i = p.i; r.pad = 0;
+  return r;
 }
 
 // final value of one output from its merged partial
@@ -617,8 +682,10 @@ std::string gen_batch_source(const nca_batch_expr& b) {
          << "  " << dtype_walker(pg.dtype) << "(it.data, c.begin, c.count, f);\n";
     }
     for (size_t a = 0; a < accs.size(); ++a) {
-      os << "  {\n    const NcaBPart m = nca_bblock<" << accs[a].kind << ", " << (accs[a].idx ? "true" : "false")
-         << ">(f.a" << a << ".part(), sh);\n    if (threadIdx.x == 0) {\n";
+      const bool f32 = b.tapes[(size_t)accs[a].tape].result_dtype == NCA_FLOAT32;
+      os << "  {\n    const NcaBPart m = " << (f32 ? "nca_bblockf<" : "nca_bblock<") << accs[a].kind << ", "
+         << (accs[a].idx ? "true" : "false") << ">(f.a" << a << (f32 ? ".partf(), sh);" : ".part(), sh);")
+         << "\n    if (threadIdx.x == 0) {\n";
       for (int o = 0; o < pg.n_outs; ++o) {
         if (acc_of_out[o] != (int)a) continue;
         const std::string none = pg.op[o] == NCA_RED_ARGMAX ? "(double)nca_blo<" + std::string(nca::jit_ctype(b.tapes[(size_t)pg.tape[o]].result_dtype)) + ">()"
