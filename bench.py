@@ -364,7 +364,42 @@ def measure_c3(torch, nca, peak, iters=10):
                         omp_threads(), reps=2)
         out[name] = op_entry(8 * n, ms, peak, elements=n, per="iteration", rel_l2_err_vs_f64=rel_l2,
                              max_err_rel_to_max=max_rel, status=status, cpu_baseline=cpu)
-        del a, b, a64, b64, t32, t64
+        # the same iteration through the general stencil (Stencil.create: the
+        # shifted views of a zero-padded (514, 514, 514) source, one fused
+        # expression per point), against the TMA kernel's first iteration
+        from ncarray_gb300.stencil import Stencil
+        wl = [float(v) for v in w.reshape(27)]
+        offs = [(i, j, k) for i in range(3) for j in range(3) for k in range(3)]
+        used = [t for t in range(27) if wl[t] != 0.0]
+
+        def lap(views, wl=wl, used=used):
+            acc = None
+            for t in used:
+                term = nca.DevExpr.leaf(views[t]) * np.float32(wl[t])
+                acc = term if acc is None else acc + term
+            return nca.DevExpr.leaf(views[13]) + acc * np.float32(0.1)
+
+        gst = Stencil.create([offs[t] for t in range(27)], lap, nca.DType.float32, is_pointer_axis=[0, 0, 0])
+        pad = nca.NCDevArray((514, 514, 514), nca.DType.float32).fill(0.0)
+        pad._buf.view(torch.float32).view(514, 514, 514)[1:513, 1:513, 1:513].copy_(src32)
+        dst = nca.NCDevArray((512, 512, 512), nca.DType.float32)
+        gst.apply(pad, dst)
+        e0.record(s)
+        for _ in range(3):
+            gst.apply(pad, dst)
+        e1.record(s)
+        torch.cuda.synchronize()
+        gms = e0.elapsed_time(e1) / 3
+        one = nca.NCDevArray((512, 512, 512), nca.DType.float32)
+        a1 = nca.NCDevArray((512, 512, 512), nca.DType.float32)
+        a1._buf.view(torch.float32).view(512, 512, 512).copy_(src32)
+        r1 = st.iterate(a1, one, 1)
+        tg = dst._buf.view(torch.float32).double()
+        tt = r1._buf.view(torch.float32).double()
+        out["general_" + name] = op_entry(4 * (514 ** 3 + n), gms, peak, elements=n, per="iteration",
+                                          offsets=len(used), kernel="nca_stencil (fused shifted views, JIT kind 2)",
+                                          max_diff_rel_to_max_vs_tma=float((tg - tt).abs().max() / tt.abs().max()))
+        del a, b, a64, b64, t32, t64, pad, dst, one, a1, tg, tt
     return out
 
 
