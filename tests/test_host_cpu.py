@@ -98,3 +98,47 @@ def test_reference_arm_other_ranks_print_nothing(capsys):
         steps, warmup, gpus = 1, 3, 2
     bench.run_reference(A(), rank=1)
     assert capsys.readouterr().out == ""
+
+
+def test_evaluate_many_merges_operands(monkeypatch):
+    """evaluate_many on the host: equal operand views of the expressions
+    become one operand, every tape's loads are renumbered into the merged
+    list, and one nca_expr_multi call carries all tapes and outputs (the C ABI
+    is replaced by a recorder: no GPU)."""
+    torch = pytest.importorskip("torch")
+    import ncarray_gb300 as nca
+    import ncarray_gb300.array as arr_mod
+    from ncarray_gb300 import _lib
+    from ncarray_gb300.dtype import ITEMSIZE, RedOp
+
+    def mk(shape, dt):
+        n = max(int(np.prod(shape)) * ITEMSIZE[dt], 1)
+        return nca.NCDevArray(shape, dt, _buf=torch.empty(n, dtype=torch.uint8))
+
+    x, v, k = mk((4, 2, 3, 8), DType.float32), mk((2,), DType.float32), mk((8, 2, 3, 4), DType.int32)
+    with nca.lazy_mode():
+        y = x.permute(3, 1, 2, 0) * v.reshape(1, 2, 1, 1) + k
+        z = (k * 3 + 7) % 11
+        w = k * k - k
+    outs = [mk(y.shape, y.dtype), mk(z.shape, z.dtype), mk(w.shape, w.dtype)]
+    mx = mk((8, 2, 4), DType.float32)
+    calls = []
+    monkeypatch.setattr(_lib, "call", lambda name, *a: calls.append((name, a)) or 0)
+    monkeypatch.setattr(arr_mod, "current_stream", lambda: 0)
+    res = nca.evaluate_many([(y, outs[0]), (z, outs[1]), (w, outs[2])], reductions=[(RedOp.MAX, 2)], red_out=[mx])
+    assert res == [mx]
+    assert [c[0] for c in calls] == ["nca_expr_multi"]
+    tarr, nt, ops, nops, oarr, rarr, nred, stream = calls[0][1]
+    assert (nt, nops, nred) == (3, 3, 1)
+    assert [ops[i].data for i in range(3)] == [x.ptr, v.ptr, k.ptr]
+    assert [oarr[i].data for i in range(3)] == [o.ptr for o in outs]
+
+    def loads(t):
+        return sorted({int(t.instrs[i]) & 0xFFFFFF for i in range(t.n_instrs) if int(t.instrs[i]) >> 24 == OpCode.LOAD_NCARR})
+
+    assert loads(tarr[0]) == [0, 1, 2]
+    assert loads(tarr[1]) == [2] and loads(tarr[2]) == [2]
+    assert rarr[0].op == int(RedOp.MAX) and rarr[0].axes_mask == 1 << 2
+    # shapes must agree
+    with pytest.raises(ValueError):
+        nca.evaluate_many([(y, outs[0]), (z, mk((8, 2, 3, 5), DType.int32))])

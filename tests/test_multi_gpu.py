@@ -150,3 +150,19 @@ def test_shared_operand_given_twice(cuda):
     assert all(g.tobytes() == w.tobytes() for g, w in zip(got, want))
     assert all(g.tobytes() == w.tobytes() for g, w in zip(got_r, want_r))
     assert launches == 1
+
+
+def test_idx_tape_falls_back(cuda):
+    """An extra tape reading the element index (IDX) is not fused: the calls
+    run in order with the same results."""
+    rng = np.random.default_rng(SEED + 1350)
+    x, v, k = _c2_like(rng)
+    dx, dv, dk = (nca.NCDevArray.from_host(a) for a in (x, v, k))
+    y, _, _, _ = _exprs(dx, dv, dk, x.shape[1])
+    with nca.lazy_mode():
+        zi = dk + nca.iota(dk, DType.int32)
+    want, want_r = _separate([y, zi], REDS)
+    got, got_r, launches = _fused([y, zi], REDS)
+    assert all(g.tobytes() == w.tobytes() for g, w in zip(got, want))
+    assert all(g.tobytes() == w.tobytes() for g, w in zip(got_r, want_r))
+    assert launches >= 2
