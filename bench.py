@@ -1159,7 +1159,8 @@ def main():
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(ms_e2e, 4),
                "how": f"CUDA-graph replays of {GS} consecutive steps, each in {NCH} chunks along axis 1 "
                       f"pipelined over {NCS} copy-in, 1 compute and {NCS} copy-out streams (pinned host "
-                      "buffers, nca_copy_host + evaluate_many on chunk views; every step copies all its inputs in "
+                      "buffers, nca_copy_host + " + ("evaluate" if C2_FORKED else "evaluate_many") +
+                      " on chunk views; every step copies all its inputs in "
                       "and all its results out)",
                "serial_ms_per_step": round(ms_serial, 4), "eager_pipelined_ms_per_step": round(ms_eager, 4),
                "matches_serial": same}
