@@ -324,6 +324,31 @@ def measure_c1(torch, nca, peak, flush_buf, reps=20):
                     l2="flushed before every rep (512 MiB write, then 256 MiB read: no dirty lines left)")
 
 
+def gst_used(w):
+    """Offsets (flat 3x3x3 indices) of the non-zero weights."""
+    return [t for t in range(27) if float(w.reshape(27)[t]) != 0.0]
+
+
+def general_laplacian(nca, w, scale=0.1):
+    """u + scale * sum_t w_t u[o_t] as ncarray's Stencil<3> over the shifted
+    views of a zero-padded source (offsets 0..2 per axis, one per non-zero
+    weight), float32."""
+    from ncarray_gb300.stencil import Stencil
+    wl = [float(v) for v in w.reshape(27)]
+    used = gst_used(w)
+    centre = used.index(13)
+
+    def lap(views):
+        acc = None
+        for k, t in enumerate(used):
+            term = nca.DevExpr.leaf(views[k]) * np.float32(wl[t])
+            acc = term if acc is None else acc + term
+        return nca.DevExpr.leaf(views[centre]) + acc * np.float32(scale)
+
+    offs = [(t // 9, (t // 3) % 3, t % 3) for t in used]
+    return Stencil.create(offs, lap, nca.DType.float32, is_pointer_axis=[0, 0, 0])
+
+
 def measure_c3(torch, nca, peak, iters=10):
     """C3: 7- and 27-point Laplacian, 512^3 float32, zero halo, 10 Jacobi steps
     u <- u + 0.1 L(u); error vs the float64 run of the same steps."""
@@ -366,38 +391,35 @@ def measure_c3(torch, nca, peak, iters=10):
                              max_err_rel_to_max=max_rel, status=status, cpu_baseline=cpu)
         # the same iteration through the general stencil (Stencil.create: the
         # shifted views of a zero-padded (514, 514, 514) source, one fused
-        # expression per point), against the TMA kernel's first iteration
-        from ncarray_gb300.stencil import Stencil
-        wl = [float(v) for v in w.reshape(27)]
-        offs = [(i, j, k) for i in range(3) for j in range(3) for k in range(3)]
-        used = [t for t in range(27) if wl[t] != 0.0]
-
-        def lap(views, wl=wl, used=used):
-            acc = None
-            for t in used:
-                term = nca.DevExpr.leaf(views[t]) * np.float32(wl[t])
-                acc = term if acc is None else acc + term
-            return nca.DevExpr.leaf(views[13]) + acc * np.float32(0.1)
-
-        gst = Stencil.create([offs[t] for t in range(27)], lap, nca.DType.float32, is_pointer_axis=[0, 0, 0])
+        # expression per point), against the TMA kernel's first iteration;
+        # timed in the tiled form (the default) and in the view form
+        gst = general_laplacian(nca, w)
         pad = nca.NCDevArray((514, 514, 514), nca.DType.float32).fill(0.0)
         pad._buf.view(torch.float32).view(514, 514, 514)[1:513, 1:513, 1:513].copy_(src32)
         dst = nca.NCDevArray((512, 512, 512), nca.DType.float32)
-        gst.apply(pad, dst)
-        e0.record(s)
-        for _ in range(3):
+        gms = {}
+        for form, mode in (("view", "0"), ("tiled", "1")):
+            os.environ["NCA_STENCIL_TILE"] = mode
             gst.apply(pad, dst)
-        e1.record(s)
-        torch.cuda.synchronize()
-        gms = e0.elapsed_time(e1) / 3
+            e0.record(s)
+            for _ in range(5):
+                gst.apply(pad, dst)
+            e1.record(s)
+            torch.cuda.synchronize()
+            gms[form] = e0.elapsed_time(e1) / 5
+        os.environ.pop("NCA_STENCIL_TILE", None)
         one = nca.NCDevArray((512, 512, 512), nca.DType.float32)
         a1 = nca.NCDevArray((512, 512, 512), nca.DType.float32)
         a1._buf.view(torch.float32).view(512, 512, 512).copy_(src32)
         r1 = st.iterate(a1, one, 1)
         tg = dst._buf.view(torch.float32).double()
         tt = r1._buf.view(torch.float32).double()
-        out["general_" + name] = op_entry(4 * (514 ** 3 + n), gms, peak, elements=n, per="iteration",
-                                          offsets=len(used), kernel="nca_stencil (fused shifted views, JIT kind 2)",
+        gbytes = 4 * (514 ** 3 + n)
+        out["general_" + name] = op_entry(gbytes, gms["tiled"], peak, elements=n, per="iteration",
+                                          offsets=len(gst_used(w)),
+                                          kernel="nca_stencil_tile (shared-memory planes, register window along z)",
+                                          view_form={"ms": round(gms["view"], 4), "GB/s": round(gbytes / gms["view"] / 1e6, 1),
+                                                     "kernel": "nca_nd (one strided view per offset)"},
                                           max_diff_rel_to_max_vs_tma=float((tg - tt).abs().max() / tt.abs().max()))
         del a, b, a64, b64, t32, t64, pad, dst, one, a1, tg, tt
     return out
@@ -835,6 +857,15 @@ def profile_op(torch, nca, op: str, steps: int) -> None:
         ds = nca.NCDevArray((n,), nca.DType.float32, _buf=src.view(torch.uint8))
         dest = nca.NCDevArray((nd,), nca.DType.float32).fill(0.0)
         fn = lambda: dest.scatter_add(di, ds)  # noqa: E731
+    elif op in ("stencil-general-7", "stencil-general-27"):
+        # the 7- / 27-point Laplacian through the general stencil on a
+        # zero-padded (322, 322, 322) float32 grid (133 MB in, 131 MB out)
+        from ncarray_gb300.stencil import laplacian7, laplacian27
+        st = general_laplacian(nca, laplacian7() if op.endswith("-7") else laplacian27())
+        src = nca.NCDevArray((322, 322, 322), nca.DType.float32)
+        src._buf.view(torch.float32).normal_()
+        out = nca.NCDevArray((320, 320, 320), nca.DType.float32)
+        fn = lambda: st.apply(src, out)  # noqa: E731
     elif op == "stencil-binning":
         # the pixel-binning stencil of the reference's benchmark through the
         # general stencil: 8 offset views of a (32, 512, 1024) float32 image

@@ -588,6 +588,10 @@ std::string jit_gen_eval(const Tape& t, const std::string& load_prefix, const st
   return gen_eval(t, load_prefix, load_suffix);
 }
 
+std::string jit_from_bits(int dtype, const std::string& bits) { return from_bits(dtype, bits); }
+std::string jit_to_bits(int dtype, const std::string& value) { return to_bits(dtype, value); }
+std::string jit_storage_uint(int size) { return storage_uint(size); }
+
 const char* jit_prelude() { return kPrelude; }
 
 static std::string lim_expr(int dt, bool lowest) {
@@ -2378,6 +2382,7 @@ int jit_selftest(const char* arch) {
     ++n;
   }
   n += batch_expr_selftest(a.c_str());
+  n += stencil_tile_selftest(a.c_str());
   return n;
 }
 

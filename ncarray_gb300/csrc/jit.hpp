@@ -66,6 +66,12 @@ std::string jit_gen_eval(const Tape& t, const std::string& load_prefix, const st
 uint64_t jit_scalar_word(int compute_dtype, int scalar_dtype, uint64_t slot);
 // C type name of an arithmetic dtype in generated device code.
 const char* jit_ctype(int dtype);
+// Generated-code expressions: the value of `dtype` held as raw bits in the
+// integer expression `bits`; the raw bits (u32, or u64 for 8 bytes) of
+// `value` stored as `dtype`; the unsigned integer type of `size` bytes.
+std::string jit_from_bits(int dtype, const std::string& bits);
+std::string jit_to_bits(int dtype, const std::string& value);
+std::string jit_storage_uint(int size);
 
 }  // namespace nca
 
@@ -74,4 +80,5 @@ int jit_selftest(const char* arch);
 // NVRTC compile of `source` for `arch` without loading it (fails on errors)
 void jit_compile_only(const std::string& source, const std::string& arch);
 int batch_expr_selftest(const char* arch);
+int stencil_tile_selftest(const char* arch);
 }
