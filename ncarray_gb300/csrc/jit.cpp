@@ -364,6 +364,8 @@ struct Spec {
   int k4r = 0;       // kind 4: row lanes per warp (row-lane form, one reduced dim rd); 0: thread per column group
   int rd = 0;
   int k4p = 0;       // kind 4 row-lane form on a persistent grid (equal contiguous ranges of units)
+  int k4b = 0;       // kind 4 row-lane form with rows bulk-copied into a shared-memory ring
+  int k4b_rb = 16, k4b_ns = 4, k4b_cb = 1;   // its rows per stage, stages, column blocks per CTA
   int k3u = 8;       // kind 3 teams: loads of a thread in flight together (8 against 4: global sum
                      // 0.79 -> 0.83, argmax over rows of 16,384 0.79 -> 0.90 of measured)
   // kind 7: extra outputs, each a tape over the same operands stored elementwise
@@ -626,7 +628,8 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_HAS_OUT " << (sp.has_out ? 1 : 0) << "\n#define NCA_NWORDS " << L.nwords
      << "\n#define NCA_HAS_SUM " << (sp.has_sum ? 1 : 0) << "\n#define NCA_HAS_MAX " << (sp.has_max ? 1 : 0)
      << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n#define NCA_LASTCTA " << sp.lastcta
-     << "\n#define NCA_K4R " << sp.k4r << "\n#define NCA_RD " << sp.rd << "\n#define NCA_K4P " << sp.k4p << "\n";
+     << "\n#define NCA_K4R " << sp.k4r << "\n#define NCA_RD " << sp.rd << "\n#define NCA_K4P " << sp.k4p
+     << "\n#define NCA_K4B " << sp.k4b << "\n";
   int sum_mode = 1;
   if (sp.nred > 0) {
     const int ra = arith_dtype(sp.r);
@@ -745,6 +748,34 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
   os << "__device__ __forceinline__ void nca_gather1(const NcaArgs& A, const i64* off, nca_w (*v)[NCA_VEC]) {\n"
      << g1.str() << "}\n";
   os << "#define nca_gather_ns nca_gather\n";
+  if (sp.kind == 4 && sp.k4b) {
+    // bulk-staged row-lane form: per operand its element size, its row
+    // segment in a stage (64 kept groups) and its offset in the stage; the
+    // lane's NCA_VEC elements of each operand read from shared memory
+    int esum = 0, off = 0;
+    std::ostringstream es_f, rb_f, of_f, sg;
+    for (int k = 0; k < sp.nops; ++k) {
+      const int dt = sp.op_dtypes[k], es = dtinfo(dt).size, rowb = 64 * sp.k4b_cb * sp.vec * es;
+      es_f << "  if (k == " << k << ") return " << es << ";\n";
+      rb_f << "  if (k == " << k << ") return " << rowb << ";\n";
+      of_f << "  if (k == " << k << ") return " << off << ";\n";
+      off += sp.k4b_rb * rowb;
+      esum += es;
+      const int bytes = es * sp.vec;
+      sg << "  { const " << vec_type(bytes) << " u = *(const " << vec_type(bytes) << "*)(p[" << k << "]);";
+      for (int q = 0; q < sp.vec; ++q)
+        sg << " v[" << k << "][" << q << "] = (nca_w)(" << from_bits(dt, lane_bits(bytes, es, q, "u")) << ");";
+      sg << " }\n";
+    }
+    os << "#define NCA_K4B_RB " << sp.k4b_rb << "\n#define NCA_K4B_NS " << sp.k4b_ns << "\n#define NCA_K4B_CB " << sp.k4b_cb
+       << "\n#define NCA_K4B_STAGE " << off
+       << "\n#define NCA_K4B_ESUM " << esum << "\n";
+    os << "__device__ __forceinline__ constexpr int nca_k4b_es(int k) {\n" << es_f.str() << "  return 0;\n}\n";
+    os << "__device__ __forceinline__ constexpr int nca_k4b_rowb(int k) {\n" << rb_f.str() << "  return 0;\n}\n";
+    os << "__device__ __forceinline__ constexpr int nca_k4b_opoff(int k) {\n" << of_f.str() << "  return 0;\n}\n";
+    os << "__device__ __forceinline__ void nca_sgather(const unsigned char* const* p, nca_w (*v)[NCA_VEC]) {\n"
+       << sg.str() << "}\n";
+  }
   // operands whose byte offsets equal an earlier operand's (same strides)
   os << "__device__ __forceinline__ constexpr int nca_sal(int k) {\n  return ";
   for (int k = 0; k < (int)sp.op_salias.size(); ++k)
@@ -1098,6 +1129,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
   add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
   add(sp.nob); add(sp.lastcta); add(sp.block); add(sp.k4r); add(sp.rd); add(sp.k4p); add(sp.k3u);
+  add(sp.k4b); add(sp.k4b_rb); add(sp.k4b_ns); add(sp.k4b_cb);
   k += literal_key(t) + '|';
   add(sp.xvec);
   for (size_t x = 0; x < sp.xtapes.size(); ++x) {
@@ -1132,7 +1164,7 @@ static CUfunction kernel_for(const Spec& sp, const Tape& t) {
     if (it != cache.end()) return it->second;
   }
   CUfunction fn = jit_get(gen_source(sp, t), kernel_name(sp.kind));
-  if (sp.kind == 6 || sp.kind == 7) {
+  if (sp.kind == 6 || sp.kind == 7 || sp.k4b) {
     // the staged class lives on shared memory: ask for the largest carveout
     check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_PREFERRED_SHARED_MEMORY_CARVEOUT, 100), "carveout");
   }
@@ -1814,6 +1846,18 @@ int reduce_out_dtype(int op, int in_dt) {
   fail(NCA_ERR_INVALID, "unknown reduction op %d", op);
 }
 
+// NCA_K4_BULK=1 puts eligible outer reductions on the bulk-staged row-lane
+// form (measured, GB300, CUDA-graph replays: sum over axis 0 of (4096, 16384)
+// float32 0.72 of measured HBM at best over 1-4 column blocks, 2-8 stages and
+// 4-32 rows per stage, against 0.73 for the plain row-lane form; max over axis
+// 1 of (256, 256, 1024) 0.79 against 0.81: the loads in flight are not what
+// bounds these shapes); any NCA_K4_ROWS setting names another form
+static bool k4b_on() {
+  const char* e = getenv("NCA_K4_BULK");
+  const char* r = getenv("NCA_K4_ROWS");
+  return e && e[0] == '1' && !(r && r[0]);
+}
+
 // NCA_K4_ROWS=0 keeps outer reductions on the thread-per-column-group form
 // unless a tuned choice names the row-lane form; NCA_K4_ROWS=2 has the
 // row-lane form merge its splits in a finalize launch instead of the last CTA
@@ -2154,6 +2198,77 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       launch_finalize(sp, tape, KN, S, sms, w, stream);
     }
   };
+  // bulk-staged row-lane form (NCA_K4_BULK=1): every operand contiguous along
+  // the kept innermost dim with 16-byte aligned rows, one reduced dim
+  // (outermost of two, or the middle of three), not float64 work (bound by
+  // its pipe, not by loads). Rows per stage for about 16 KB, 4 stages; splits
+  // so that every CTA is resident at once (a CTA per set and split)
+  bool bulk_ok = rows_ok && k4b_on() && arith_dtype(tape.compute_dtype) != NCA_FLOAT64 &&
+                 ((s.nd == 2 && rdim == 0) || (s.nd == 3 && rdim == 1));
+  for (int k = 0; k < nops && bulk_ok; ++k) {
+    const CArr& a = s.ops[k];
+    const int es = dtinfo(a.dtype).size, vb = es * sp.vec;
+    if (sp.op_modes[k] != M_CONTIG || a.st[s.nd - 1] != es || (vb != 4 && vb != 8 && vb != 16)) bulk_ok = false;
+    else if ((uintptr_t)a.base % 16 || a.st[rdim] % 16 || (s.nd == 3 && a.st[0] % 16) || (s.shape[s.nd - 1] * es) % 16)
+      bulk_ok = false;
+  }
+  if (bulk_ok && s.shape[s.nd - 1] % sp.vec) bulk_ok = false;
+  if (bulk_ok) {
+    const int R = 4, GPC = 64;
+    const int64_t inner = s.shape[s.nd - 1];
+    sp.unroll = 1;
+    sp.k4r = R;
+    sp.rd = rdim;
+    sp.k4b = 1;
+    // column blocks: up to 4 KB of each row per CTA while the sets still
+    // give every SM a CTA
+    sp.k4b_cb = 1;
+    for (int cb : {4, 2}) {
+      const int64_t sets = cdiv(inner / sp.vec, (int64_t)GPC * cb) * (s.nd == 3 ? s.shape[0] : 1);
+      if (inner / sp.vec >= (int64_t)GPC * cb && (sets * std::max<int64_t>(1, RN / 64) >= sms)) { sp.k4b_cb = cb; break; }
+    }
+    if (const char* e = getenv("NCA_K4B_CB")) { const int v = atoi(e); if (v == 1 || v == 2 || v == 4) sp.k4b_cb = v; }
+    int rowsum = 0;
+    for (int k = 0; k < nops; ++k) rowsum += GPC * sp.k4b_cb * sp.vec * dtinfo(s.ops[k].dtype).size;
+    sp.k4b_rb = std::max(R, std::min(64, 16384 / rowsum / R * R));
+    sp.k4b_ns = 4;
+    if (const char* e = getenv("NCA_K4B_RB")) { const int v = atoi(e); if (v >= R && v <= 256 && v % R == 0) sp.k4b_rb = v; }
+    if (const char* e = getenv("NCA_K4B_NS")) { const int v = atoi(e); if (v >= 2 && v <= 8) sp.k4b_ns = v; }
+    const int64_t smem = (int64_t)sp.k4b_ns * sp.k4b_rb * rowsum + 16 * sp.k4b_ns;
+    if (smem <= 200 * 1024) {
+      const int64_t nset = cdiv(inner / sp.vec, (int64_t)GPC * sp.k4b_cb) * (s.nd == 3 ? s.shape[0] : 1);
+      // resident CTAs per SM of the form (the merging variant; the other has the same footprint)
+      sp.lastcta = 1;
+      CUfunction fn = kernel_for(sp, tape);
+      check_cu(drv().cuFuncSetAttribute(fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)smem), "smem attribute");
+      int per_sm = 0;
+      check_cu(drv().cuOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 288, (size_t)smem), "occupancy");
+      int64_t S = std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * std::max(per_sm, 1) / nset, RN / sp.k4b_rb));
+      const int64_t C = cdiv(RN, S);
+      S = cdiv(RN, C);
+      if (S == 1) { sp.lastcta = 0; fn = kernel_for(sp, tape); }
+      const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
+      std::vector<uint64_t> w;
+      fill_common_words(s, sp, tape, L, w);
+      w[L.nsplit] = (uint64_t)S; w[L.chunk] = (uint64_t)C; w[L.keptn] = (uint64_t)KN; w[L.redn] = (uint64_t)RN;
+      const size_t pbytes = S > 1 ? (size_t)(S * KN) * 8 * ((has_sum ? 1 : 0) + (has_max ? 2 : 0) + (has_min ? 2 : 0)) : 0;
+      const size_t cbytes = sp.lastcta ? ((size_t)nset * 4 + 255) / 256 * 256 : 0;
+      StreamScratch part(pbytes + cbytes, stream);
+      if (S > 1) {
+        uint64_t* p = (uint64_t*)part.ptr;
+        if (has_sum) { w[L.psum] = (uint64_t)(uintptr_t)p; p += S * KN; }
+        if (has_max) { w[L.pmax] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+        if (has_min) { w[L.pmin] = (uint64_t)(uintptr_t)p; p += 2 * S * KN; }
+        w[L.aux] = (uint64_t)(uintptr_t)p;
+        check_cuda(cudaMemsetAsync(p, 0, cbytes, stream), "arrival counters");
+      }
+      launch(fn, nset * S, w, stream, (unsigned)smem, 288);
+      return true;
+    }
+    sp.k4r = 0;
+    sp.rd = 0;
+    sp.k4b = 0;
+  }
   // schedule: the autotuner's cached choice for this (dtypes, ops, stored
   // value, kept and reduced size class, dims), else 4 rows in flight and 1024
   // threads per SM; searched (rows 4 / 8, 512 / 1024 / 2048 threads per SM)
@@ -2290,6 +2405,10 @@ int jit_selftest(const char* arch) {
         ++n;
         s4.lastcta = 0; s4.k4p = 1;    // on a persistent grid
         nvrtc_compile(gen_source(s4, t), a);
+        ++n;
+        Spec s5 = sp;                  // rows bulk-copied into a shared-memory ring
+        s5.k4r = 4; s5.rd = 1; s5.k4b = 1; s5.lastcta = 1; s5.k4b_cb = 2;
+        nvrtc_compile(gen_source(s5, t), a);
         ++n;
       }
     }
