@@ -590,6 +590,11 @@ std::string jit_gen_eval(const Tape& t, const std::string& load_prefix, const st
   return gen_eval(t, load_prefix, load_suffix);
 }
 
+std::string jit_gen_eval_w(const Tape& t, const std::string& load_prefix, const std::string& load_suffix,
+                           const std::string& W) {
+  return gen_eval(t, load_prefix, load_suffix, W);
+}
+
 std::string jit_from_bits(int dtype, const std::string& bits) { return from_bits(dtype, bits); }
 std::string jit_to_bits(int dtype, const std::string& value) { return to_bits(dtype, value); }
 std::string jit_storage_uint(int size) { return storage_uint(size); }

@@ -62,6 +62,9 @@ CUfunction jit_get(const std::string& source, const char* name);
 // `nca_w` ending in `return` (operand k loaded as prefix + k + suffix).
 const char* jit_prelude();
 std::string jit_gen_eval(const Tape& t, const std::string& load_prefix, const std::string& load_suffix);
+// the same over the type named W (its operations specialised by the caller)
+std::string jit_gen_eval_w(const Tape& t, const std::string& load_prefix, const std::string& load_suffix,
+                           const std::string& W);
 // A tape scalar as the 64-bit argument word of compute dtype `compute_dtype`.
 uint64_t jit_scalar_word(int compute_dtype, int scalar_dtype, uint64_t slot);
 // C type name of an arithmetic dtype in generated device code.

@@ -89,6 +89,7 @@ struct TilePlan {
   bool cpa = true;                        // cp.async staging (4- and 8-byte elements)
   bool off32 = false;                     // in-plane byte offsets fit 32 bits
   int minb = 0;                           // __launch_bounds__ minimum CTAs per SM (0: none)
+  bool pk = false;                        // float32 tape on column pairs (i, i + 1) in f32x2 instructions
   std::vector<int> dz, dy, dx;            // per operand: its normalised offset
   // a cell: one (row of the thread's VY-row strip plus dy, dx) position, with
   // the z offsets read there; read at several, it has a register window
@@ -143,6 +144,36 @@ std::string tile_source(const TilePlan& P, const Tape& t, int src_dt, int dst_dt
   os << "struct NcaStArgs { u64 w[" << 14 + std::max(nscal, 1) << "]; };\n";
   os << "__device__ __forceinline__ nca_w nca_sv(const nca_w* v, const u64* s) {\n  (void)s; const i64 lin = 0; (void)lin;\n"
      << jit_gen_eval(t, "v[", "]") << "}\n";
+  if (P.pk) {
+    // two float32 lanes per instruction: add, sub and multiply each as one
+    // packed fused multiply-add (a + b = fma(a, 1, b), a - b = fma(b, -1, a),
+    // a * b = fma(a, b, -0): one rounding, signed zeros as IEEE add, sub and
+    // mul; a separate packed mul and add could be contracted into one fma),
+    // division, negation and absolute value lane by lane
+    os << "struct nca_f2 { u64 v; };   // lanes x (low word) and y\n"
+       << "__device__ __forceinline__ u64 nca_pk2(float x, float y) { u64 r; asm(\"mov.b64 %0, {%1, %2};\" : \"=l\"(r) : \"f\"(x), \"f\"(y)); return r; }\n"
+       << "__device__ __forceinline__ float nca_lo2(u64 r) { float x, y; asm(\"mov.b64 {%0, %1}, %2;\" : \"=f\"(x), \"=f\"(y) : \"l\"(r)); return x; }\n"
+       << "__device__ __forceinline__ float nca_hi2(u64 r) { float x, y; asm(\"mov.b64 {%0, %1}, %2;\" : \"=f\"(x), \"=f\"(y) : \"l\"(r)); return y; }\n"
+       << "template <> __device__ __forceinline__ nca_f2 nca_word<nca_f2>(u64 b) { const float f = __uint_as_float((u32)b); return {nca_pk2(f, f)}; }\n";
+    // the constant pairs (1, 1), (-1, -1), (-0, -0) are read from device
+    // memory so that the assembler cannot see them and turn the fma back into
+    // a mul or an add
+    os << "__device__ u64 nca_f2c[3] = {0x3f8000003f800000ull, 0xbf800000bf800000ull, 0x8000000080000000ull};\n"
+       << "__device__ __forceinline__ nca_f2 nca_f2fma(u64 a, u64 b, u64 c) { u64 d; asm(\"fma.rn.f32x2 %0, %1, %2, %3;\" "
+          ": \"=l\"(d) : \"l\"(a), \"l\"(b), \"l\"(c)); return {d}; }\n";
+    const char* pops[][2] = {{"nca_add", "nca_f2fma(a.v, nca_f2c[0], b.v)"},
+                             {"nca_sub", "nca_f2fma(b.v, nca_f2c[1], a.v)"},
+                             {"nca_mul", "nca_f2fma(a.v, b.v, nca_f2c[2])"},
+                             {"nca_mulc", "nca_f2fma(a.v, b.v, nca_f2c[2])"}};
+    for (auto& o : pops)
+      os << "template <> __device__ __forceinline__ nca_f2 " << o[0] << "<nca_f2>(nca_f2 a, nca_f2 b) { return " << o[1]
+         << "; }\n";
+    os << "template <> __device__ __forceinline__ nca_f2 nca_div<nca_f2>(nca_f2 a, nca_f2 b) { return {nca_pk2(nca_div<float>(nca_lo2(a.v), nca_lo2(b.v)), nca_div<float>(nca_hi2(a.v), nca_hi2(b.v)))}; }\n"
+       << "template <> __device__ __forceinline__ nca_f2 nca_neg<nca_f2>(nca_f2 a) { return {nca_pk2(nca_neg<float>(nca_lo2(a.v)), nca_neg<float>(nca_hi2(a.v)))}; }\n"
+       << "template <> __device__ __forceinline__ nca_f2 nca_abs<nca_f2>(nca_f2 a) { return {nca_pk2(nca_abs<float>(nca_lo2(a.v)), nca_abs<float>(nca_hi2(a.v)))}; }\n";
+    os << "__device__ __forceinline__ nca_f2 nca_sv2(const nca_f2* v, const u64* s) {\n  (void)s;\n"
+       << jit_gen_eval_w(t, "v[", "]", "nca_f2") << "}\n";
+  }
   os << "__device__ __forceinline__ nca_w nca_sl(nca_s b) { return (nca_w)(" << jit_from_bits(src_dt, "b") << "); }\n";
   os << "__device__ __forceinline__ void nca_sput(char* p, nca_w e) { *(" << D << "*)p = (" << D << ")"
      << jit_to_bits(dst_dt, "e") << "; }\n";
@@ -200,7 +231,8 @@ std::string tile_source(const TilePlan& P, const Tape& t, int src_dt, int dst_dt
   for (int c = 0; c < ncell; ++c)
     if (P.cells[(size_t)c].win)
       for (int m = 0; m < P.sz; ++m)
-        for (int i = 0; i < P.vx; ++i) os << "  nca_w w" << c << "_" << m << "_" << i << " = (nca_w)0;\n";
+        for (int i = 0; i < P.vx; i += P.pk ? 2 : 1)
+          os << "  " << (P.pk ? "u64" : "nca_w") << " w" << c << "_" << m << "_" << i << " = 0;\n";
   os << "  for (int k = 0; k < " << P.pd << "; ++k) NCA_ST_ISSUE();\n";
   os << "  const int lb = ty * " << P.vy * pc << " + tx;\n";
   os << "  for (int jb = 0; jb < J; jb += " << P.sz << ") {\n";
@@ -219,7 +251,10 @@ std::string tile_source(const TilePlan& P, const Tape& t, int src_dt, int dst_dt
     for (int c = 0; c < ncell; ++c)
       if (P.cells[(size_t)c].win)
         for (int i = 0; i < P.vx; ++i)
-          os << "      w" << c << "_" << u << "_" << i << " = nca_sl(pl[" << at(c, i) << "]);\n";
+          if (!P.pk) os << "      w" << c << "_" << u << "_" << i << " = nca_sl(pl[" << at(c, i) << "]);\n";
+          else if (i % 2 == 0)
+            os << "      w" << c << "_" << u << "_" << i << " = nca_pk2(nca_sl(pl[" << at(c, i) << "]), nca_sl(pl["
+               << at(c, i + 1) << "]));\n";
     os << "      if (j >= " << P.sz - 1 << ") {\n";
     for (int b = 0; b < P.sz; ++b)
       if (back_used[(size_t)b])
@@ -228,23 +263,57 @@ std::string tile_source(const TilePlan& P, const Tape& t, int src_dt, int dst_dt
     for (int c = 0; c < ncell; ++c)
       if (!P.cells[(size_t)c].win)
         for (int i = 0; i < P.vx; ++i)
-          os << "        const nca_w d" << c << "_" << i << " = nca_sl(pb" << P.sz - 1 - P.cells[(size_t)c].zs[0] << "["
-             << at(c, i) << "]);\n";
-    for (int i = 0; i < P.vx; ++i)
+          if (!P.pk)
+            os << "        const nca_w d" << c << "_" << i << " = nca_sl(pb" << P.sz - 1 - P.cells[(size_t)c].zs[0] << "["
+               << at(c, i) << "]);\n";
+          else if (i % 2 == 0)
+            os << "        const u64 d" << c << "_" << i << " = nca_pk2(nca_sl(pb" << P.sz - 1 - P.cells[(size_t)c].zs[0]
+               << "[" << at(c, i) << "]), nca_sl(pb" << P.sz - 1 - P.cells[(size_t)c].zs[0] << "[" << at(c, i + 1) << "]));\n";
+    auto operand = [&](int k, int i, int jj) {
+      const int c = P.cell_of[(size_t)k * (size_t)P.vy + (size_t)jj];
+      if (P.cells[(size_t)c].win) return "w" + std::to_string(c) + "_" + std::to_string((u + 1 + P.dz[(size_t)k]) % P.sz) +
+                                        "_" + std::to_string(i);
+      return "d" + std::to_string(c) + "_" + std::to_string(i);
+    };
+    for (int i = 0; i < P.vx; i += P.pk ? 2 : 1)
       for (int jj = 0; jj < P.vy; ++jj) {
-        os << "        if (ok" << i << "_" << jj << ") {\n          const nca_w v[" << P.dz.size() << "] = {";
-        for (size_t k = 0; k < P.dz.size(); ++k) {
-          const int c = P.cell_of[k * (size_t)P.vy + (size_t)jj];
-          os << (k ? ", " : "");
-          if (P.cells[(size_t)c].win) os << "w" << c << "_" << (u + 1 + P.dz[k]) % P.sz << "_" << i;
-          else os << "d" << c << "_" << i;
+        const std::string a = std::to_string(i) + "_" + std::to_string(jj), b = std::to_string(i + 1) + "_" + std::to_string(jj);
+        if (P.pk) {
+          os << "        if (ok" << a << " || ok" << b << ") {\n          const nca_f2 v[" << P.dz.size() << "] = {";
+          for (size_t k = 0; k < P.dz.size(); ++k)
+            os << (k ? ", " : "") << "{" << operand((int)k, i, jj) << "}";
+          os << "};\n          const u64 r = nca_sv2(v, s).v;\n"
+             << "          if (ok" << a << ") nca_sput(db + dzo + oo" << a << ", nca_lo2(r));\n"
+             << "          if (ok" << b << ") nca_sput(db + dzo + oo" << b << ", nca_hi2(r));\n        }\n";
+          continue;
         }
-        os << "};\n          nca_sput(db + dzo + oo" << i << "_" << jj << ", nca_sv(v, s));\n        }\n";
+        os << "        if (ok" << a << ") {\n          const nca_w v[" << P.dz.size() << "] = {";
+        for (size_t k = 0; k < P.dz.size(); ++k) os << (k ? ", " : "") << operand((int)k, i, jj);
+        os << "};\n          nca_sput(db + dzo + oo" << a << ", nca_sv(v, s));\n        }\n";
       }
     os << "      }\n      dzo += dsz;\n      rst = rst + 1 == " << nst << " ? 0 : rst + 1;\n    }\n";
   }
   os << "  }\n  asm volatile(\"cp.async.wait_group 0;\\n\" ::: \"memory\");\n}\n";
   return os.str();
+}
+
+// NCA_STENCIL_TILE_PK=1 and a tape that reads only operands and constants and
+// applies only add, sub, mul, div, neg and abs (the operations of the
+// column-pair evaluator). Opt-in: measured on GB300 (512^3 float32, padded
+// source) the 27-point Laplacian at 2830 GB/s against 3417 one column at a
+// time, the 7-point at 4824 against 5055 (the pairs need more registers and
+// the packed fma issues no faster than two float32 instructions here).
+bool pk_tape(const Tape& t) {
+  const char* e = getenv("NCA_STENCIL_TILE_PK");
+  if (!(e && e[0] == '1')) return false;
+  for (uint32_t ins : t.instrs) {
+    switch ((int)(ins >> 24)) {
+      case NCA_OP_NOOP: case NCA_OP_LOAD_NCARR: case NCA_OP_LOAD_SOARR: case NCA_OP_LOAD_CONST: case NCA_OP_ADD:
+      case NCA_OP_SUB: case NCA_OP_MUL: case NCA_OP_DIV: case NCA_OP_NEG: case NCA_OP_ABS: break;
+      default: return false;
+    }
+  }
+  return true;
 }
 
 // The offset set and tape as a tile plan (host only); null when they fit,
@@ -269,17 +338,21 @@ const char* plan_tile(const int64_t* offsets, int n, int nd, const Tape& t, Tile
     for (int d = 0; d < nd; ++d) o[lead + d] = (int)(offsets[(int64_t)k * nd + d] - mn[lead + d]);
     P.dz.push_back(o[0]); P.dy.push_back(o[1]); P.dx.push_back(o[2]);
   }
+  // float32 tapes of add, sub, mul, div, neg and abs, when asked for: column
+  // pairs in f32x2 instructions (two columns per thread, 32 apart)
+  P.pk = arith_dtype(t.compute_dtype) == NCA_FLOAT32 && pk_tape(t);
   // the tallest strip (4, 2 or 1 rows per thread) whose register window
-  // stays within 64 registers; a wide window (over 32 registers) in CTAs of
-  // 4 warps, at least 4 per SM, else CTAs of 8 warps, at least 2 per SM
+  // stays within 64 registers (80 for column pairs); a wide window (over 32
+  // registers) in CTAs of 4 warps, at least 4 per SM, else CTAs of 8 warps,
+  // at least 2 per SM
   const int wsize = dtinfo(t.compute_dtype).size;
-  P.vx = 1;
+  P.vx = P.pk ? 2 : 1;
   for (int vy : {4, 2, 1}) {
     P.vy = vy;
     plan_cells(P);
-    if (P.window_regs(wsize) <= 64) break;
+    if (P.window_regs(wsize) <= (P.pk ? 80 : 64)) break;
   }
-  const int wregs = P.window_regs(wsize);
+  const int wregs = P.window_regs(wsize) / P.vx;
   if (wregs > 96) return "a register window over 96 registers";
   P.by = wregs > 32 ? 4 : 8;
   P.minb = wregs > 32 ? 4 : 2;
@@ -343,6 +416,7 @@ bool stencil_tile(const nca_view& src, const nca_view& dest, const int64_t* step
         v[1] >= 1 && v[1] <= 8 && (v[2] == 2 || v[2] == 4 || v[2] == 8 || v[2] == 16) && v[3] >= 1 && v[3] <= 8 &&
         v[4] >= 1 && v[5] >= 0 && v[5] <= 16) {
       P.vx = v[0]; P.vy = v[1]; P.by = v[2]; P.pd = v[3]; P.zc = v[4]; P.minb = v[5];
+      if (P.vx % 2) P.pk = false;
       zc_set = true;
       plan_cells(P);
     }
@@ -382,7 +456,7 @@ bool stencil_tile(const nca_view& src, const nca_view& dest, const int64_t* step
   // the plan: compiled source per (tape, offsets, dtypes, tile)
   std::ostringstream key;
   key << dev << '|' << src.dtype << '|' << dest.dtype << '|' << t.compute_dtype << '|' << P.vx << P.vy << ',' << P.by
-      << ',' << P.pd << ',' << P.zc << ',' << P.cpa << P.off32 << ',' << P.minb << '|' << P.sz << P.sy << P.sx << '|';
+      << ',' << P.pd << ',' << P.zc << ',' << P.cpa << P.off32 << P.pk << ',' << P.minb << '|' << P.sz << P.sy << P.sx << '|';
   for (int k = 0; k < n; ++k) key << P.dz[(size_t)k] << ',' << P.dy[(size_t)k] << ',' << P.dx[(size_t)k] << ';';
   key << '|';
   for (uint32_t ins : t.instrs) key << ins << ',';
@@ -423,8 +497,9 @@ bool stencil_tile(const nca_view& src, const nca_view& dest, const int64_t* step
 }  // namespace
 
 // Compile-only check of tiled stencil plans for `arch`: the 7- and 27-point
-// float32 Laplacians, a float64 3x3x3 set, an int32 tape over asymmetric
-// offsets, bfloat16 staged by plain loads, and a 2-D 5-point set.
+// float32 Laplacians (the latter on column pairs), a float64 3x3x3 set, an
+// int32 tape over asymmetric offsets, bfloat16 staged by plain loads, and a
+// 2-D 5-point set.
 int stencil_tile_selftest(const char* arch) {
   auto I = [](int op, int idx) { return (uint32_t)(op << 24) | (uint32_t)idx; };
   // sum of c * v_k over n operands, then + v_0
@@ -466,6 +541,11 @@ int stencil_tile_selftest(const char* arch) {
     P.cpa = c.cpa;
     P.zc = 64;
     P.off32 = n % 2 == 0;
+    if (n == 1) {   // the 27-point set on column pairs
+      P.pk = true;
+      P.vx = 2;
+      plan_cells(P);
+    }
     jit_compile_only(tile_source(P, t, c.src, c.dst, 1), arch);
     ++n;
   }

@@ -184,3 +184,25 @@ def test_where_the_tiled_form_does_not_apply(cuda):
     out = nca.NCDevArray((7, 15, 31), DType.float32)
     st.apply(P, out)
     assert np.array_equal(out.to_host(), np.zeros((7, 15, 31), np.float32))
+
+
+@pytest.mark.parametrize("w", ["7", "27"])
+def test_column_pairs_opt_in(cuda, orc, w):
+    """NCA_STENCIL_TILE_PK=1: float32 tapes evaluated on column pairs in packed
+    f32x2 fused multiply-adds, bit for bit the view form and the oracle."""
+    rng = np.random.default_rng(SEED + 1460 + int(w))
+    shape = (21, 70, 150)
+    pad = np.zeros((shape[0] + 2, shape[1] + 2, shape[2] + 2), np.float32)
+    pad[1:-1, 1:-1, 1:-1] = rng.normal(size=shape)
+    st = _laplacian_stencil(laplacian7() if w == "7" else laplacian27(), DType.float32, 0.1)
+    src = nca.NCDevArray.from_host(pad)
+    with _env(NCA_STENCIL_TILE_PK="1"):
+        tiled, view = _both(st, src, shape, DType.float32)
+    assert tiled.tobytes() == view.tobytes()
+    assert tiled.tobytes() == oracle_stencil(orc, st, pad, 10, shape, 10).tobytes()
+    # a tape with division, negation and absolute value
+    st2 = Stencil.create([(0, 0, 0), (1, 1, 1), (2, 2, 2)], lambda v: -abs(v[0] - v[1]) / (v[2] * np.float32(3.0) + 7.0),
+                         DType.float32)
+    with _env(NCA_STENCIL_TILE_PK="1"):
+        tiled, view = _both(st2, src, shape, st2.result_dtype)
+    assert tiled.tobytes() == view.tobytes()
