@@ -366,6 +366,8 @@ struct Spec {
   int k4p = 0;       // kind 4 row-lane form on a persistent grid (equal contiguous ranges of units)
   int k4b = 0;       // kind 4 row-lane form with rows bulk-copied into a shared-memory ring
   int k4b_rb = 16, k4b_ns = 4, k4b_cb = 1;   // its rows per stage, stages, column blocks per CTA
+  int k3rv = 0, k3tu = 1;   // kind 3 one-thread teams: reduced vectors per unit (compile time; 0: runtime
+                            // loop) and units whose operands a thread gathers before reducing them
   int k3u = 8;       // kind 3 teams: loads of a thread in flight together (8 against 4: global sum
                      // 0.79 -> 0.83, argmax over rows of 16,384 0.79 -> 0.90 of measured)
   // kind 7: extra outputs, each a tape over the same operands stored elementwise
@@ -634,7 +636,7 @@ static std::string gen_source(const Spec& sp, const Tape& t) {
      << "\n#define NCA_HAS_SUM " << (sp.has_sum ? 1 : 0) << "\n#define NCA_HAS_MAX " << (sp.has_max ? 1 : 0)
      << "\n#define NCA_HAS_MIN " << (sp.has_min ? 1 : 0) << "\n#define NCA_LASTCTA " << sp.lastcta
      << "\n#define NCA_K4R " << sp.k4r << "\n#define NCA_RD " << sp.rd << "\n#define NCA_K4P " << sp.k4p
-     << "\n#define NCA_K4B " << sp.k4b << "\n";
+     << "\n#define NCA_K4B " << sp.k4b << "\n#define NCA_K3RV " << sp.k3rv << "\n#define NCA_K3TU " << sp.k3tu << "\n";
   int sum_mode = 1;
   if (sp.nred > 0) {
     const int ra = arith_dtype(sp.r);
@@ -1134,7 +1136,7 @@ static std::string plan_key(const Spec& sp, const Tape& t) {
   add(sp.rb); add(sp.tmask); add(sp.tile_bytes); add(sp.unroll); add(sp.qxp); add(sp.minb); add(sp.grp);
   add(sp.ns); add(sp.ld); add(sp.npc); add(sp.ltp8); add(sp.pmask); add(sp.umask); add(sp.nmaps); add(sp.uumask); add(sp.ptrmask);
   add(sp.nob); add(sp.lastcta); add(sp.block); add(sp.k4r); add(sp.rd); add(sp.k4p); add(sp.k3u);
-  add(sp.k4b); add(sp.k4b_rb); add(sp.k4b_ns); add(sp.k4b_cb);
+  add(sp.k4b); add(sp.k4b_rb); add(sp.k4b_ns); add(sp.k4b_cb); add(sp.k3rv); add(sp.k3tu);
   k += literal_key(t) + '|';
   add(sp.xvec);
   for (size_t x = 0; x < sp.xtapes.size(); ++x) {
@@ -2006,6 +2008,18 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       C = cdiv(C, sp.vec) * sp.vec;
       if (C > 0) S = cdiv(RN, C);
       if (S < 1) S = 1;
+      // one-thread teams over at most 8 vectors, no splits, no pointer
+      // operands: a thread gathers the operands of 2 units before reducing
+      // either (NCA_K3_UNITS: 1 keeps one unit at a time; the binning
+      // reshape-sum of (32, 512, 1024) float32 at 1 / 2 / 4 / 8 units: 0.56 /
+      // 0.66 / 0.60 / 0.49 of measured HBM)
+      sp.k3rv = 0;
+      sp.k3tu = 1;
+      if (sp.team == 1 && S == 1 && sp.ptrmask == 0 && RN > 0 && RN % sp.vec == 0 && RN / sp.vec <= 8) {
+        int tu = 2;
+        if (const char* e = getenv("NCA_K3_UNITS")) tu = std::max(1, std::min(8, atoi(e)));
+        if (tu > 1) { sp.k3rv = (int)(RN / sp.vec); sp.k3tu = tu; }
+      }
       const WordLayout L = word_layout(sp.nops, sp.nd, sp.nscal, sp.nred, sp.ptrmask != 0);
       std::vector<uint64_t> w;
       fill_common_words(s, sp, tape, L, w);
@@ -2390,6 +2404,11 @@ int jit_selftest(const char* arch) {
         s1.team = 1;
         nvrtc_compile(gen_source(s1, t), a);
         ++n;
+        if (kind == 3) {               // and its form that gathers 4 units of 2 vectors at once
+          s1.k3rv = 2; s1.k3tu = 4;
+          nvrtc_compile(gen_source(s1, t), a);
+          ++n;
+        }
       }
       if (kind == 3 || kind == 5) {   // two-thread teams; the warp-per-position finalize
         Spec s2 = sp;
