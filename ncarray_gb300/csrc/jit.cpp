@@ -2011,8 +2011,8 @@ bool expr_reduce(const Tape& tape, const nca_view* ops, int nops, const nca_view
       // one-thread teams over at most 8 vectors, no splits, no pointer
       // operands: a thread gathers the operands of 2 units before reducing
       // either (NCA_K3_UNITS: 1 keeps one unit at a time; the binning
-      // reshape-sum of (32, 512, 1024) float32 at 1 / 2 / 4 / 8 units: 0.56 /
-      // 0.66 / 0.60 / 0.49 of measured HBM)
+      // reshape-sum of (32, 512, 1024) float32 at 1 / 2 / 3 / 4 / 8 units:
+      // 0.56 / 0.66-0.68 / 0.60 / 0.60 / 0.49 of measured HBM)
       sp.k3rv = 0;
       sp.k3tu = 1;
       if (sp.team == 1 && S == 1 && sp.ptrmask == 0 && RN > 0 && RN % sp.vec == 0 && RN / sp.vec <= 8) {
